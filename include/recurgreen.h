@@ -1,0 +1,140 @@
+/*
+ * recurgreen.h -- C ABI of the GB300-native recursive Green-function sweep.
+ *
+ * A drop-in for the `waveguide` module of RecurGreen (src/waveguide.f90): the
+ * same ten waveguide parameters, one transmission computation per disorder
+ * realization, and the transmission-eigenvalue distribution task.  Every entry
+ * point takes plain pointers and sizes; all arithmetic is IEEE double /
+ * double complex (complex values are interleaved (re, im) pairs, matrices are
+ * column-major with leading dimension = number of rows, as in Fortran).
+ *
+ * Error convention: every call returns an int status (RG_OK == 0).  The
+ * reference prints a message and stops the process (src/base_utils.f90:56-57,
+ * src/waveguide.f90:91-142,408-421); here the message is kept in a
+ * thread-local buffer returned by rg_last_error() and the caller decides.
+ *
+ * Threading: a handle, like a Fortran `waveguide_t` object, is not shared
+ * between host threads (src/main.f90:148-150 gives each OpenMP thread its own
+ * copy).  Each handle owns one CUDA stream and its device buffers.
+ */
+#ifndef RECURGREEN_H
+#define RECURGREEN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define RG_OK 0
+#define RG_ERR_INVALID_ARG 1  /* stop errmsg_invalid_arg in the reference */
+#define RG_ERR_SINGULAR 2     /* zgetrf info > 0 / zero or NaN pivot */
+#define RG_ERR_CUDA 3         /* CUDA runtime failure (message has details) */
+#define RG_ERR_NOMEM 4        /* host or device allocation failed */
+#define RG_ERR_NOCONV 5       /* singular-value iteration did not converge */
+
+/* Transverse boundary conditions (src/waveguide.f90:150-236). */
+#define RG_BOUND_DIRICHLET 0
+#define RG_BOUND_PERIODIC 1
+
+/* The `&waveguide` namelist (src/main.f90:83), plus `ny`: the number of
+ * transverse grid points.  ny == 0 keeps the reference's ny = nmu
+ * (src/waveguide.f90:162,202). */
+typedef struct rg_params {
+  int boundtype; /* RG_BOUND_DIRICHLET or RG_BOUND_PERIODIC */
+  int nxdiso;    /* slices in the disordered region */
+  int nxfree;    /* free slices on each side */
+  double wol;    /* W / lambda */
+  double exfac;  /* mode-basis extension factor, in [1, 1e4] */
+  double aratio; /* L / W */
+  double dscat;  /* L / l_scat */
+  double dabso;  /* L / l_abso */
+  double napera; /* fraction of controlled modes (input port a), in (0, 1] */
+  double naperb; /* fraction of observed modes (output port b), in (0, 1] */
+  int ny;        /* transverse grid points; 0 => nmu */
+} rg_params;
+
+typedef struct rg_waveguide rg_waveguide;
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* rg_last_error(void);
+
+/* init_waveguide (src/waveguide.f90:81-255): validates the parameters and
+ * builds the mode set, mumesh, dos and the B diagonal on the current CUDA
+ * device.  Warnings the reference prints (Shannon limit, weak disorder) are
+ * not errors here either. */
+int rg_init(const rg_params* params, rg_waveguide** out);
+
+/* init_copy_waveguide (src/waveguide.f90:262-270). */
+int rg_init_copy(const rg_waveguide* src, rg_waveguide** out);
+
+/* del_waveguide (src/waveguide.f90:275-286).  Accepts NULL. */
+void rg_del(rg_waveguide* wg);
+
+/* Getters: get_nmu, get_neigv, get_nx (src/waveguide.f90:291-320), plus the
+ * derived sizes the reference keeps private (ny, nprop and the filtering
+ * window imin..imax x jmin..jmax, 1-based as in Fortran). */
+int rg_get_nmu(const rg_waveguide* wg);
+int rg_get_neigv(const rg_waveguide* wg);
+int rg_get_nx(const rg_waveguide* wg);
+int rg_get_ny(const rg_waveguide* wg);
+int rg_get_nprop(const rg_waveguide* wg);
+int rg_get_window(const rg_waveguide* wg, int* imin, int* imax, int* jmin, int* jmax);
+/* get_xmesh (src/waveguide.f90:325-329): len must equal nx. */
+int rg_get_xmesh(const rg_waveguide* wg, double* xmesh, int64_t len);
+/* get_parameters (src/waveguide.f90:335-350). */
+int rg_get_parameters(const rg_waveguide* wg, rg_params* out);
+/* Internal scalars of the reference object: kdx, dos and the standard
+ * deviation stdu of the dimensionless potential (src/waveguide.f90:118,243,370). */
+int rg_get_scalars(const rg_waveguide* wg, double* kdx, double* dos, double* stdu);
+
+/* compute_tdistrib (src/waveguide.f90:392-462): draws the disorder of seed
+ * `iseed`, runs the recursive Green sweep on the GPU, and writes the neigv
+ * transmission eigenvalues (descending) into chunk iseed of the host array
+ * tallvals[len].  Same checks as the reference: len must be a positive
+ * multiple of neigv and 1 <= iseed <= len / neigv. */
+int rg_compute_tdistrib(rg_waveguide* wg, int iseed, double* tallvals, int64_t len);
+
+/* compute_refl_trans_v1 (src/waveguide.f90:469-519): full nmu x nmu
+ * transmission matrix t (and, if rmat != NULL, reflection matrix r) of seed
+ * iseed, Fisher-Lee with sqrt(real(mu)).  Host buffers of nmu*nmu complex
+ * doubles, column-major. */
+int rg_compute_refl_trans_v1(rg_waveguide* wg, int iseed, double* rmat, double* tmat);
+
+/* As rg_compute_tdistrib / rg_compute_refl_trans_v1, but for a caller-given
+ * potential upot(nxdiso, ny) (host, column-major: x fastest), already scaled
+ * by stdu as set_hamiltonian_waveguide stores it (src/waveguide.f90:366-372).
+ * teigvals receives neigv values; tfilt, if not NULL, the filtered Fisher-Lee
+ * t of tdistrib ((imax-imin+1) x (jmax-jmin+1) complex, column-major). */
+int rg_tdistrib_upot(rg_waveguide* wg, const double* upot, double* teigvals, double* tfilt);
+int rg_refl_trans_v1_upot(rg_waveguide* wg, const double* upot, double* rmat, double* tmat);
+
+/* The potential of seed iseed as the GPU draws it (host output, nxdiso*ny
+ * doubles, column-major), for inspection and tests. */
+int rg_potential(rg_waveguide* wg, int iseed, double* upot);
+
+/* Batched tdistrib (the OpenMP seed loop of src/main.f90:134-179, as one
+ * persistent launch): realization k uses seed seeds[k] and writes its neigv
+ * eigenvalues to tallvals[k*neigv ...].  Host pointers; status[k] (may be
+ * NULL) receives the per-realization status.  Returns the first non-OK
+ * status, after every realization has run. */
+int rg_tdistrib_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* tallvals, int32_t* status);
+
+/* Same on device pointers, enqueued on `stream` (a cudaStream_t; NULL means
+ * the handle's own stream).  Synchronises the stream before returning. */
+int rg_tdistrib_batch_device(rg_waveguide* wg, const int32_t* d_seeds, int n, double* d_tallvals,
+                             int32_t* d_status, void* stream);
+
+/* histogram (src/base_utils.f90:491-516) with the reference's exact edge
+ * semantics, computed on the GPU: samples[n] and bins[nbins+1] are host
+ * arrays; histo[nbins] and *missing receive counts as doubles. */
+int rg_histogram(const double* samples, int64_t n, const double* bins, int nbins, double* histo,
+                 double* missing);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RECURGREEN_H */

@@ -1,0 +1,217 @@
+"""GB300-native recursive Green-function sweep of RecurGreen.
+
+Python mirror of the reference ``waveguide`` module interface
+(src/waveguide.f90:13-73) over the C ABI in ``include/recurgreen.h``
+(``librecurgreen_gb300.so``, built in-tree by ``recurgreen_gb300.build``).
+All computation runs in the CUDA library; this module only moves arguments.
+If the library is missing, every entry point raises: there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "librecurgreen_gb300.so")
+_LIB = None
+
+RG_OK, RG_ERR_INVALID_ARG, RG_ERR_SINGULAR, RG_ERR_CUDA, RG_ERR_NOMEM, RG_ERR_NOCONV = range(6)
+BOUNDTYPES = {"dirichlet": 0, "periodic": 1}
+
+# Every symbol declared in include/recurgreen.h.
+EXPORTS = (
+    "rg_last_error", "rg_init", "rg_init_copy", "rg_del", "rg_get_nmu", "rg_get_neigv", "rg_get_nx",
+    "rg_get_ny", "rg_get_nprop", "rg_get_window", "rg_get_xmesh", "rg_get_parameters", "rg_get_scalars",
+    "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
+    "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
+)
+
+
+class RecurGreenError(RuntimeError):
+    """A non-zero status from the C ABI (the reference would have stopped)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[status {code}] {msg}")
+        self.code = code
+
+
+class rg_params(C.Structure):
+    _fields_ = [("boundtype", C.c_int), ("nxdiso", C.c_int), ("nxfree", C.c_int), ("wol", C.c_double),
+                ("exfac", C.c_double), ("aratio", C.c_double), ("dscat", C.c_double), ("dabso", C.c_double),
+                ("napera", C.c_double), ("naperb", C.c_double), ("ny", C.c_int)]
+
+
+def lib() -> C.CDLL:
+    """Loads the CUDA library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise RecurGreenError(RG_ERR_CUDA, f"{LIB_PATH} is missing; run `python -m recurgreen_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, ip, i64 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int64
+    L.rg_last_error.restype = C.c_char_p
+    L.rg_init.argtypes = [C.POINTER(rg_params), C.POINTER(vp)]
+    L.rg_init_copy.argtypes = [vp, C.POINTER(vp)]
+    L.rg_del.argtypes = [vp]
+    L.rg_del.restype = None
+    for f in ("rg_get_nmu", "rg_get_neigv", "rg_get_nx", "rg_get_ny", "rg_get_nprop"):
+        getattr(L, f).argtypes = [vp]
+    L.rg_get_window.argtypes = [vp] + [C.POINTER(C.c_int)] * 4
+    L.rg_get_xmesh.argtypes = [vp, dp, i64]
+    L.rg_get_parameters.argtypes = [vp, C.POINTER(rg_params)]
+    L.rg_get_scalars.argtypes = [vp, dp, dp, dp]
+    L.rg_compute_tdistrib.argtypes = [vp, C.c_int, dp, i64]
+    L.rg_compute_refl_trans_v1.argtypes = [vp, C.c_int, vp, vp]
+    L.rg_tdistrib_upot.argtypes = [vp, dp, dp, vp]
+    L.rg_refl_trans_v1_upot.argtypes = [vp, dp, vp, vp]
+    L.rg_potential.argtypes = [vp, C.c_int, dp]
+    L.rg_tdistrib_batch.argtypes = [vp, ip, C.c_int, dp, ip]
+    L.rg_tdistrib_batch_device.argtypes = [vp, vp, C.c_int, vp, vp, vp]
+    L.rg_histogram.argtypes = [dp, i64, dp, C.c_int, dp, dp]
+    _LIB = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != RG_OK:
+        raise RecurGreenError(rc, lib().rg_last_error().decode())
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Waveguide:
+    """The reference ``waveguide_t`` on the GPU.
+
+    ``Waveguide(boundtype, nxdiso, nxfree, wol, exfac, aratio, dscat, dabso,
+    napera, naperb)`` mirrors ``init`` (src/waveguide.f90:81-85); ``ny`` is
+    the optional transverse grid size (0 keeps the reference's ny = nmu).
+    """
+
+    def __init__(self, boundtype: str = "dirichlet", nxdiso: int = 100, nxfree: int = 0, wol: float = 4.3,
+                 exfac: float = 1.0, aratio: float = 1.0, dscat: float = 1.0, dabso: float = 0.0,
+                 napera: float = 1.0, naperb: float = 1.0, ny: int = 0, _handle=None):
+        L = lib()
+        if _handle is None:
+            p = rg_params(BOUNDTYPES.get(boundtype, -1), nxdiso, nxfree, wol, exfac, aratio, dscat, dabso,
+                          napera, naperb, ny)
+            h = C.c_void_p()
+            _check(L.rg_init(C.byref(p), C.byref(h)))
+            _handle = h
+        self._h = _handle
+        self.nmu = L.rg_get_nmu(self._h)
+        self.neigv = L.rg_get_neigv(self._h)
+        self.nx = L.rg_get_nx(self._h)
+        self.ny = L.rg_get_ny(self._h)
+        self.nprop = L.rg_get_nprop(self._h)
+        w = [C.c_int() for _ in range(4)]
+        _check(L.rg_get_window(self._h, *[C.byref(x) for x in w]))
+        self.imin, self.imax, self.jmin, self.jmax = (x.value for x in w)
+        p = self.get_parameters()
+        self.nxdiso, self.nxfree = p["nxdiso"], p["nxfree"]
+        s = [C.c_double() for _ in range(3)]
+        _check(L.rg_get_scalars(self._h, *[C.byref(x) for x in s]))
+        self.kdx, self.dos, self.stdu = (x.value for x in s)
+
+    # -- construction / destruction (src/waveguide.f90:262-286) --
+    def init_copy(self) -> "Waveguide":
+        h = C.c_void_p()
+        _check(lib().rg_init_copy(self._h, C.byref(h)))
+        return Waveguide(_handle=h)
+
+    def delete(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().rg_del(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.delete()
+        except Exception:
+            pass
+
+    # -- getters (src/waveguide.f90:291-350) --
+    def get_nmu(self) -> int:
+        return self.nmu
+
+    def get_neigv(self) -> int:
+        return self.neigv
+
+    def get_nx(self) -> int:
+        return self.nx
+
+    def get_xmesh(self) -> np.ndarray:
+        x = np.zeros(self.nx, np.float64)
+        _check(lib().rg_get_xmesh(self._h, _dp(x), x.size))
+        return x
+
+    def get_parameters(self) -> dict:
+        p = rg_params()
+        _check(lib().rg_get_parameters(self._h, C.byref(p)))
+        bt = {v: k for k, v in BOUNDTYPES.items()}[p.boundtype]
+        return dict(boundtype=bt, nxdiso=p.nxdiso, nxfree=p.nxfree, wol=p.wol, exfac=p.exfac, aratio=p.aratio,
+                    dscat=p.dscat, dabso=p.dabso, napera=p.napera, naperb=p.naperb, ny=p.ny)
+
+    # -- computations --
+    def compute_tdistrib(self, iseed: int, tallvals: np.ndarray) -> None:
+        """compute_tdistrib (src/waveguide.f90:392-462): fills chunk iseed of tallvals in place."""
+        if tallvals.dtype != np.float64 or not tallvals.flags.c_contiguous:
+            raise RecurGreenError(RG_ERR_INVALID_ARG, "tallvals must be a contiguous float64 array")
+        _check(lib().rg_compute_tdistrib(self._h, int(iseed), _dp(tallvals), tallvals.size))
+
+    def compute_refl_trans_v1(self, iseed: int) -> np.ndarray:
+        """t of compute_refl_trans_v1 (src/waveguide.f90:469-519), nmu x nmu complex."""
+        t = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_compute_refl_trans_v1(self._h, int(iseed), None, t.ctypes.data))
+        return t
+
+    def tdistrib_upot(self, upot: np.ndarray, want_t: bool = False):
+        """Eigenvalues (and the filtered Fisher-Lee t) for a given potential
+        upot (shape (ny, nxdiso) C-order == upot(nxdiso, ny) Fortran order)."""
+        upot = np.ascontiguousarray(upot, np.float64)
+        if upot.shape != (self.ny, self.nxdiso):
+            raise RecurGreenError(RG_ERR_INVALID_ARG, f"upot must have shape {(self.ny, self.nxdiso)}")
+        T = np.zeros(self.neigv, np.float64)
+        t = np.zeros((self.imax - self.imin + 1, self.jmax - self.jmin + 1), np.complex128, order="F")
+        _check(lib().rg_tdistrib_upot(self._h, _dp(upot), _dp(T), t.ctypes.data if want_t else None))
+        return (T, t) if want_t else T
+
+    def refl_trans_v1_upot(self, upot: np.ndarray) -> np.ndarray:
+        upot = np.ascontiguousarray(upot, np.float64)
+        if upot.shape != (self.ny, self.nxdiso):
+            raise RecurGreenError(RG_ERR_INVALID_ARG, f"upot must have shape {(self.ny, self.nxdiso)}")
+        t = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_refl_trans_v1_upot(self._h, _dp(upot), None, t.ctypes.data))
+        return t
+
+    def potential(self, iseed: int) -> np.ndarray:
+        """The disorder of seed iseed as drawn on the GPU, shape (ny, nxdiso)."""
+        u = np.zeros((self.ny, self.nxdiso), np.float64)
+        _check(lib().rg_potential(self._h, int(iseed), _dp(u)))
+        return u
+
+    def tdistrib_batch(self, seeds, return_status: bool = False):
+        """Batched compute_tdistrib: eigenvalues of every seed, shape (n * neigv,)."""
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        out = np.zeros(seeds.size * self.neigv, np.float64)
+        st = np.zeros(seeds.size, np.int32)
+        ip = C.POINTER(C.c_int32)
+        rc = lib().rg_tdistrib_batch(self._h, seeds.ctypes.data_as(ip), seeds.size, _dp(out), st.ctypes.data_as(ip))
+        if return_status:
+            return out, st
+        _check(rc)
+        return out
+
+
+def histogram(samples, bins):
+    """histogram (src/base_utils.f90:491-516) on the GPU -> (histo, missing)."""
+    samples = np.ascontiguousarray(samples, np.float64)
+    bins = np.ascontiguousarray(bins, np.float64)
+    h = np.zeros(max(bins.size - 1, 0), np.float64)
+    miss = C.c_double(0)
+    _check(lib().rg_histogram(_dp(samples), samples.size, _dp(bins), bins.size - 1, _dp(h), C.byref(miss)))
+    return h, miss.value

@@ -1,0 +1,79 @@
+// Internal declarations shared by the host side (rg_waveguide.cpp) and the
+// kernels (rg_sweep.cu).  Not part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/recurgreen.h"
+
+namespace rg {
+
+using cplx = std::complex<double>;
+
+// Error plumbing: the thread-local message behind rg_last_error().
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define RG_CUDA(call)                                          \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return ::rg::cuda_fail(e_, #call); \
+  } while (0)
+
+// Largest mode count the shared-memory sweep kernel handles.
+constexpr int kMaxModesSmem = 64;
+
+// Everything one launch of the sweep kernel needs.  Device pointers.
+struct SweepArgs {
+  int M;        // nmu
+  int ny;       // transverse grid points
+  int nx;       // total slices
+  int nxdiso;   // disordered slices
+  int nxfree;   // free slices on each side
+  int row0, nrow, col0, ncol;  // Fisher-Lee window, 0-based start and extent
+  int neigv;    // eigenvalues kept per realization
+  int mode;     // kModeEig or kModeTmat
+  int nreal;    // realizations in this launch
+  const double2* bmat;        // [M] B diagonal
+  const double2* adiag_edge;  // [M] A diagonal on slices 1 and nx
+  const double2* adiag_bulk;  // [M] A diagonal in the bulk
+  const double2* sqmu;        // [M] Fisher-Lee weights
+  const double* costab;       // [(2M+1) * ny] cos(pi d y_j) / ny  (Dirichlet)
+  const double2* expfac;      // [M * ny] exp(2 pi i d y_j) / ny  (periodic), d = 0..M-1
+  int periodic;
+  const double* upot;         // potential, element (r, ix, iy) at r*pot_rstride + ix*pot_xstride + iy*pot_ystride
+  int64_t pot_rstride, pot_xstride, pot_ystride;
+  double* teig;               // [nreal * neigv] (kModeEig)
+  double2* tout;              // [nreal * nrow * ncol] column-major t (optional)
+  int32_t* status;            // [nreal]
+  int* work_counter;          // persistent-scheduling counter, zeroed before launch
+};
+
+constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
+constexpr int kModeTmat = 1;  // v1 t only: full t written to tout
+
+// Potential generator arguments.
+struct PotArgs {
+  int nxdiso, ny, nreal;
+  double stdu;
+  const int32_t* seeds;        // [nreal]
+  const uint64_t* jumppoly;    // [ny * 4] x^(2*nxdiso*iy) mod charpoly
+  double* upot;                // [nreal][nxdiso][ny]
+};
+
+// Launchers (rg_sweep.cu).  All enqueue on `stream`.
+int launch_potential(const PotArgs& a, cudaStream_t stream);
+int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count);
+int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
+                     unsigned long long* d_counts, cudaStream_t stream);
+
+// xoshiro256** jump-ahead polynomials (rg_waveguide.cpp).
+void jump_polynomial(uint64_t distance, uint64_t out[4]);
+
+}  // namespace rg

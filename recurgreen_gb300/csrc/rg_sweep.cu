@@ -1,0 +1,536 @@
+// GB300 (sm_103a) kernels of the recursive Green-function sweep.
+//
+//   potential_kernel  -- the disorder U(x, y) of each seed, drawn with the
+//                        gfortran-style xoshiro256** stream of the reference
+//                        (src/random_normal.f90:40-67), one thread per
+//                        transverse point using jump-ahead polynomials.
+//   sweep_kernel      -- one realization per CTA, persistent over a work
+//                        queue: per slice the projection of U onto the modes
+//                        (src/waveguide.f90:377-380), then a pivoted complex
+//                        Gauss-Jordan elimination that yields both
+//                        Gss = inv(A - B Gss B) and Gs1 = -Gss B Gs1
+//                        (src/waveguide.f90:426-440, src/base_utils.f90:235-274),
+//                        Fisher-Lee t (src/waveguide.f90:443-445, :510) and the
+//                        eigenvalues of t^H t by one-sided Jacobi
+//                        (src/waveguide.f90:448-449, src/base_utils.f90:341-380).
+//   histogram_kernel  -- histogram with the exact edge semantics of
+//                        src/base_utils.f90:491-516.
+//
+// Everything is IEEE FP64.  On GB300 the FP64 pipe (about 1 TFLOP/s for the
+// whole chip) is the roofline of the sweep; shared memory, registers and HBM
+// have ample headroom, so the kernel keeps each slice matrix resident in
+// shared memory and spends its FP64 operations only on the elimination.
+#include "rg_internal.h"
+
+namespace rg {
+namespace {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// w - f * r with four FMAs.
+__device__ __forceinline__ double2 cfms(double2 w, double2 f, double2 r) {
+  return make_double2(fma(-f.x, r.x, fma(f.y, r.y, w.x)), fma(-f.x, r.y, fma(-f.y, r.x, w.y)));
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+
+// ---------------------------------------------------------------------------
+// Disorder generator
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+struct Xoshiro {
+  uint64_t s0, s1, s2, s3;
+  __device__ __forceinline__ void step() {
+    const uint64_t t = s1 << 17;
+    s2 ^= s0;
+    s3 ^= s1;
+    s1 ^= s2;
+    s0 ^= s3;
+    s2 ^= t;
+    s3 = rotl64(s3, 45);
+  }
+  __device__ __forceinline__ uint64_t next() {
+    const uint64_t r = rotl64(s1 * 5, 7) * 9;
+    step();
+    return r;
+  }
+};
+
+// Seed array of random_seed(put=) from the ANSI-C LCG (randi_ansic,
+// src/random_normal.f90:20-31), scrambled into the 256-bit state the way
+// gfortran's runtime does it (last put element first, XOR keys).
+__device__ Xoshiro seeded_state(int32_t seed) {
+  uint32_t s = (uint32_t)seed, put[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    s = 1103515245u * s + 12345u;
+    put[i] = s;
+  }
+  const uint64_t k0 = 0xbd0c5b6e50c2df49ULL, k1 = 0xd46061cd46e1df38ULL;
+  const uint64_t k2 = 0xbb4f4d4ed6103544ULL, k3 = 0x114a583d0756ad39ULL;
+  Xoshiro x;
+  x.s0 = ((uint64_t)put[7] | ((uint64_t)put[6] << 32)) ^ k0;
+  x.s1 = ((uint64_t)put[5] | ((uint64_t)put[4] << 32)) ^ k1;
+  x.s2 = ((uint64_t)put[3] | ((uint64_t)put[2] << 32)) ^ k2;
+  x.s3 = ((uint64_t)put[1] | ((uint64_t)put[0] << 32)) ^ k3;
+  return x;
+}
+
+// Thread (iy, r): column iy of realization r.  The reference stream is
+// upot(ix, iy) = normal[ix + iy * nxdiso] (reshape, src/waveguide.f90:372),
+// each normal consuming two uniforms, so column iy starts 2*nxdiso*iy draws
+// into the stream: the state is advanced by the jump polynomial for that
+// distance (x^d mod the characteristic polynomial, evaluated by Horner).
+__global__ void potential_kernel(PotArgs a) {
+  const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (iy >= a.ny || r >= a.nreal) return;
+  Xoshiro st = seeded_state(a.seeds[r]);
+  const uint64_t* poly = a.jumppoly + 4 * (int64_t)iy;
+  Xoshiro acc{0, 0, 0, 0};
+  for (int w = 0; w < 4; ++w) {
+    const uint64_t pw = poly[w];
+    for (int b = 0; b < 64; ++b) {
+      if ((pw >> b) & 1ULL) {
+        acc.s0 ^= st.s0; acc.s1 ^= st.s1; acc.s2 ^= st.s2; acc.s3 ^= st.s3;
+      }
+      st.step();
+    }
+  }
+  st = acc;
+  const double twopi = 2.0 * 3.141592653589793;
+  double* out = a.upot + (int64_t)r * a.nxdiso * a.ny + iy;
+  for (int ix = 0; ix < a.nxdiso; ++ix) {
+    const double u1 = (double)(st.next() >> 11) * 0x1.0p-53;
+    const double u2 = (double)(st.next() >> 11) * 0x1.0p-53;
+    out[(int64_t)ix * a.ny] = a.stdu * (sqrt(-2.0 * log(u1)) * cos(twopi * u2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sweep kernel
+// ---------------------------------------------------------------------------
+//
+// Shared memory holds the augmented matrix [W | R] (M x 2M complex, row
+// stride LD = 2*MCAP + 1 to spread banks).  W is the slice matrix being
+// inverted in place by Gauss-Jordan; R is the right-hand side B*Gs1, which
+// turns into the new propagator column Gs1 during the same elimination.
+//
+// Pivoting is implicit: rows are never swapped.  Step k picks, among rows
+// not yet used, the one with the largest |re|+|im| in column k (the izamax
+// rule of zgetrf), scales it, and eliminates column k from every other row.
+// After M steps row piv[a] of R holds row a of inv(X) * R, and W holds
+// inv(X) with rows and columns permuted.  The next slice keeps each R row in
+// place: physical row q of the next augmented matrix carries logical row
+// pinv[q], so R is only rescaled, and W is rebuilt by a row-local gather.
+template <int MCAP, int NT>
+struct SweepSmem {
+  static constexpr int LD = 2 * MCAP + 1;
+  static size_t bytes(int ny) {
+    const int nyp = (ny + 1) & ~1;
+    return sizeof(double2) * ((size_t)MCAP * LD + MCAP + 2 * MCAP) + sizeof(double) * (2 * MCAP + 2 + nyp) +
+           sizeof(int) * 5 * MCAP;
+  }
+};
+
+template <int MCAP, int NT>
+__global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
+  constexpr int NW = NT / 32;
+  constexpr int LD = SweepSmem<MCAP, NT>::LD;
+  constexpr int AMAX = (MCAP + NW - 1) / NW;  // rows per warp
+  constexpr int BMAX = (2 * MCAP + 31) / 32;  // augmented columns per lane
+  extern __shared__ double2 smem[];
+  double2* aug = smem;                         // [MCAP][LD]
+  double2* colbuf = aug + MCAP * LD;           // [MCAP]   column k before the update
+  double2* rowbuf = colbuf + MCAP;             // [2*MCAP] scaled pivot row
+  double* cc = (double*)(rowbuf + 2 * MCAP);   // [2*MCAP+2] projection coefficients
+  double* urow = cc + (2 * MCAP + 2);          // [ny] potential of the slice
+  int* piv = (int*)(urow + ((a.ny + 1) & ~1)); // [MCAP] pivot row of column k
+  int* pinv = piv + MCAP;                      // [MCAP] column of which row q was pivot
+  int* sinv = pinv + MCAP;                     // [MCAP] physical row of logical row c
+  int* colmap = sinv + MCAP;                   // [MCAP] W column holding Gss column c
+  int* used = colmap + MCAP;                   // [MCAP]
+  __shared__ int s_r, s_p, s_status, s_rot;
+  __shared__ double2 s_d;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int M = a.M, M2 = 2 * a.M;
+
+  for (;;) {
+    if (tid == 0) s_r = atomicAdd(a.work_counter, 1);
+    __syncthreads();
+    const int r = s_r;
+    if (r >= a.nreal) break;
+    if (tid == 0) s_status = RG_OK;
+    for (int c = tid; c < M; c += NT) {
+      sinv[c] = c;
+      used[c] = 0;
+    }
+    const double* U = a.upot + (int64_t)r * a.pot_rstride;
+    __syncthreads();
+
+    for (int n = 0; n < a.nx; ++n) {
+      const int id = n - a.nxfree;
+      const bool dis = (id >= 0 && id < a.nxdiso);
+      if (dis) {
+        // 1. Projection coefficients of this slice's potential.
+        for (int j = tid; j < a.ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+        __syncthreads();
+        if (!a.periodic) {
+          // cc[d] = (1/ny) sum_j U_j cos(pi d y_j), d = 0..2M, so that
+          // (modal^T diag(U) modal)[a][c] = cc[|a-c|] - cc[a+c+2].
+          const int nd = M2 + 1;
+          for (int d = tid; d < nd; d += NT) {
+            const double* ct = a.costab + d;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int j = 0;
+            for (; j + 4 <= a.ny; j += 4) {
+              s0 = fma(ct[(int64_t)(j + 0) * nd], urow[j + 0], s0);
+              s1 = fma(ct[(int64_t)(j + 1) * nd], urow[j + 1], s1);
+              s2 = fma(ct[(int64_t)(j + 2) * nd], urow[j + 2], s2);
+              s3 = fma(ct[(int64_t)(j + 3) * nd], urow[j + 3], s3);
+            }
+            for (; j < a.ny; ++j) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
+            cc[d] = (s0 + s1) + (s2 + s3);
+          }
+        } else {
+          // f[d] = (1/ny) sum_j U_j exp(2 pi i d y_j), d = 0..M-1, so that
+          // (modal^H diag(U) modal)[a][c] = f[c-a] (c >= a), conj(f[a-c]) else.
+          for (int d = tid; d < M; d += NT) {
+            const double2* et = a.expfac + d;
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < a.ny; ++j) {
+              const double2 e = et[(int64_t)j * M];
+              sr = fma(e.x, urow[j], sr);
+              si = fma(e.y, urow[j], si);
+            }
+            cc[2 * d] = sr;
+            cc[2 * d + 1] = si;
+          }
+        }
+        __syncthreads();
+      }
+
+      // 2. Assemble X = A_n - V_n - B Gss B in physical row order, and the
+      //    right-hand side R = B Gs1 (identity on the first slice).
+      const double2* adiag = (n == 0 || n == a.nx - 1) ? a.adiag_edge : a.adiag_bulk;
+      const double rsign = (n == 1) ? 1.0 : -1.0;  // Gs1 = +Gss after slice 1, -Gss B Gs1 after
+      for (int ai = 0; ai < AMAX; ++ai) {
+        const int q = warp + NW * ai;
+        if (q >= M) break;
+        const int al = (n == 0) ? q : pinv[q];  // logical row carried by physical row q
+        const double2 ba = a.bmat[al];
+        double2 v[BMAX];
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) {
+          const int J = lane + 32 * b;
+          double2 x = make_double2(0.0, 0.0);
+          if (J < M) {
+            const int c = J;
+            if (al == c) x = adiag[c];
+            if (dis) {
+              double2 vac;
+              if (!a.periodic) {
+                const int dd = al > c ? al - c : c - al;
+                vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
+              } else {
+                vac = (c >= al) ? make_double2(cc[2 * (c - al)], cc[2 * (c - al) + 1])
+                                : make_double2(cc[2 * (al - c)], -cc[2 * (al - c) + 1]);
+              }
+              x = csub(x, vac);
+            }
+            if (n > 0) {
+              const double2 g = aug[q * LD + colmap[c]];
+              x = csub(x, cmul(cmul(ba, g), a.bmat[c]));
+            }
+          } else if (J < M2) {
+            if (n == 0) {
+              x = make_double2(J - M == q ? 1.0 : 0.0, 0.0);
+            } else {
+              x = cmul(ba, cscale(rsign, aug[q * LD + J]));
+            }
+          }
+          v[b] = x;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) {
+          const int J = lane + 32 * b;
+          if (J < M2) aug[q * LD + J] = v[b];
+        }
+      }
+      __syncthreads();
+
+      // 3. Gauss-Jordan elimination with implicit partial pivoting.
+      for (int k = 0; k < M; ++k) {
+        if (warp == 0) {
+          double best = -1.0;
+          int bi = 0x7fffffff;
+          for (int i = lane; i < M; i += 32) {
+            const double2 x = aug[i * LD + k];
+            colbuf[i] = x;
+            if (!used[i]) {
+              const double m = fabs(x.x) + fabs(x.y);
+              if (m > best) {
+                best = m;
+                bi = i;
+              }
+            }
+          }
+#pragma unroll
+          for (int off = 16; off; off >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) {
+              best = ob;
+              bi = oi;
+            }
+          }
+          if (lane == 0) {
+            double2 d = make_double2(0.0, 0.0);
+            if (!(best > 0.0)) {  // zero or NaN column: numerically singular
+              s_status = RG_ERR_SINGULAR;
+              if (bi >= M) {
+                bi = 0;
+                while (bi < M - 1 && used[bi]) ++bi;
+              }
+            } else {
+              const double2 z = colbuf[bi];
+              const double den = z.x * z.x + z.y * z.y;
+              d = make_double2(z.x / den, -z.y / den);
+            }
+            used[bi] = 1;
+            piv[k] = bi;
+            pinv[bi] = k;
+            s_p = bi;
+            s_d = d;
+          }
+        }
+        __syncthreads();
+        const int p = s_p;
+        const double2 d = s_d;
+        for (int J = tid; J < M2; J += NT) rowbuf[J] = (J == k) ? d : cmul(aug[p * LD + J], d);
+        __syncthreads();
+        double2 rv[BMAX];
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) {
+          const int J = lane + 32 * b;
+          rv[b] = (J < M2) ? rowbuf[J] : make_double2(0.0, 0.0);
+        }
+        for (int ai = 0; ai < AMAX; ++ai) {
+          const int i = warp + NW * ai;
+          if (i >= M) break;
+          double2* row = aug + i * LD;
+          if (i == p) {
+#pragma unroll
+            for (int b = 0; b < BMAX; ++b) {
+              const int J = lane + 32 * b;
+              if (J < M2) row[J] = rv[b];
+            }
+          } else {
+            const double2 f = colbuf[i];
+#pragma unroll
+            for (int b = 0; b < BMAX; ++b) {
+              const int J = lane + 32 * b;
+              if (J < M2) {
+                const double2 w = (J == k) ? make_double2(0.0, 0.0) : row[J];
+                row[J] = cfms(w, f, rv[b]);
+              }
+            }
+          }
+        }
+        __syncthreads();
+      }
+
+      // 4. Permutation bookkeeping for the next slice.
+      for (int c = tid; c < M; c += NT) {
+        const int cm = pinv[sinv[c]];
+        sinv[c] = piv[c];
+        colmap[c] = cm;
+        used[c] = 0;
+      }
+      __syncthreads();
+    }
+
+    // 5. Fisher-Lee: Gs1[a][j] = sign * R[piv[a]][j]; t = 2i sqmu_a Gs1 sqmu_j.
+    const double gsign = (a.nx >= 2) ? -1.0 : 1.0;
+    const int nrow = a.nrow, ncol = a.ncol;
+    double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
+    for (int e = tid; e < nrow * ncol; e += NT) {
+      const int i = e % nrow, j = e / nrow;
+      const int gi = a.row0 + i, gj = a.col0 + j;
+      const double2 g = cscale(gsign, aug[piv[gi] * LD + M + gj]);
+      const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
+      const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);  // (0, 2) * v
+      if (tout) tout[e] = t;
+      if (a.mode == kModeEig) aug[i * LD + j] = t;
+    }
+    __syncthreads();
+
+    if (a.mode == kModeEig) {
+      // 6. Eigenvalues of t^H t by one-sided (Hestenes) Jacobi on the
+      //    vectors of the smaller dimension: columns of t if nrow >= ncol,
+      //    else rows (the singular values of t^T equal those of t).
+      const bool bycol = nrow >= ncol;
+      const int nv = bycol ? ncol : nrow;
+      const int L = bycol ? nrow : ncol;
+      const int es = bycol ? LD : 1;  // element stride inside a vector
+      const int vs = bycol ? 1 : LD;  // stride between vectors
+      const int NP = (nv + 1) & ~1;
+      const double tol = 2.220446049250313e-16 * L;
+      int sweep = 0;
+      for (; sweep < 60; ++sweep) {
+        if (tid == 0) s_rot = 0;
+        __syncthreads();
+        for (int rr = 0; rr < NP - 1; ++rr) {
+          for (int pk = warp; pk < NP / 2; pk += NW) {
+            const int pos1 = pk, pos2 = NP - 1 - pk;
+            const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
+            const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
+            if (vp >= nv || vq >= nv) continue;
+            double2* xp = aug + vp * vs;
+            double2* xq = aug + vq * vs;
+            double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+            for (int i = lane; i < L; i += 32) {
+              const double2 u = xp[i * es], w = xq[i * es];
+              al = fma(u.x, u.x, fma(u.y, u.y, al));
+              be = fma(w.x, w.x, fma(w.y, w.y, be));
+              gr = fma(u.x, w.x, fma(u.y, w.y, gr));   // re(conj(u) w)
+              gi = fma(u.x, w.y, fma(-u.y, w.x, gi));  // im(conj(u) w)
+            }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              al += __shfl_xor_sync(0xffffffffu, al, off);
+              be += __shfl_xor_sync(0xffffffffu, be, off);
+              gr += __shfl_xor_sync(0xffffffffu, gr, off);
+              gi += __shfl_xor_sync(0xffffffffu, gi, off);
+            }
+            const double ga = sqrt(gr * gr + gi * gi);
+            if (ga > tol * sqrt(al * be) && ga > 1e-300) {
+              if (lane == 0) s_rot = 1;
+              const double zeta = (be - al) / (2.0 * ga);
+              const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
+                                                  : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+              const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+              const double2 ph = make_double2(gr / ga, -gi / ga);  // exp(-i phi), gamma = |gamma| exp(i phi)
+              for (int i = lane; i < L; i += 32) {
+                const double2 u = xp[i * es];
+                const double2 w = cmul(ph, xq[i * es]);
+                xp[i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
+                xq[i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
+              }
+            }
+          }
+          __syncthreads();
+        }
+        if (!s_rot) break;
+        __syncthreads();
+      }
+      if (sweep == 60 && tid == 0) s_status = RG_ERR_NOCONV;
+      // T_k = |v_k|^2, sorted descending into teig.
+      for (int k = warp; k < nv; k += NW) {
+        const double2* xk = aug + k * vs;
+        double s = 0.0;
+        for (int i = lane; i < L; i += 32) {
+          const double2 u = xk[i * es];
+          s = fma(u.x, u.x, fma(u.y, u.y, s));
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) cc[k] = s;
+      }
+      __syncthreads();
+      for (int k = tid; k < nv; k += NT) {
+        const double tk = cc[k];
+        int rank = 0;
+        for (int j = 0; j < nv; ++j) {
+          const double tj = cc[j];
+          rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+        }
+        if (rank < a.neigv) a.teig[(int64_t)r * a.neigv + rank] = tk;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) a.status[r] = s_status;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Histogram
+// ---------------------------------------------------------------------------
+__global__ void histogram_kernel(const double* __restrict__ x, int64_t n, const double* __restrict__ bins,
+                                 int nbins, unsigned long long* counts) {
+  extern __shared__ unsigned long long hs[];  // [nbins + 1]; the last slot counts missing samples
+  for (int i = threadIdx.x; i <= nbins; i += blockDim.x) hs[i] = 0ULL;
+  __syncthreads();
+  const double b0 = bins[0], bn = bins[nbins];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[e];
+    if (v < b0 || bn < v) {
+      atomicAdd(&hs[nbins], 1ULL);
+    } else if (v == bn) {
+      atomicAdd(&hs[nbins - 1], 1ULL);
+    } else if (v == v) {  // NaN is neither counted nor missing
+      int lo = 1, hi = nbins;  // first edge index in [1, nbins] with v < bins[idx]
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (v < bins[mid]) hi = mid;
+        else lo = mid + 1;
+      }
+      atomicAdd(&hs[lo - 1], 1ULL);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= nbins; i += blockDim.x)
+    if (hs[i]) atomicAdd(&counts[i], hs[i]);
+}
+
+template <int MCAP, int NT>
+int launch_sweep_t(const SweepArgs& a, cudaStream_t stream, int sm_count) {
+  const size_t smem = SweepSmem<MCAP, NT>::bytes(a.ny);
+  RG_CUDA(cudaFuncSetAttribute(sweep_kernel<MCAP, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<MCAP, NT>, NT, smem));
+  if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "sweep kernel does not fit on an SM (ny too large?)");
+  int grid = per_sm * sm_count;
+  if (grid > a.nreal) grid = a.nreal;
+  sweep_kernel<MCAP, NT><<<grid, NT, smem, stream>>>(a);
+  RG_CUDA(cudaGetLastError());
+  return RG_OK;
+}
+
+}  // namespace
+
+int launch_potential(const PotArgs& a, cudaStream_t stream) {
+  if (a.nreal <= 0) return RG_OK;
+  dim3 block(128), grid((a.ny + 127) / 128, a.nreal);
+  potential_kernel<<<grid, block, 0, stream>>>(a);
+  RG_CUDA(cudaGetLastError());
+  return RG_OK;
+}
+
+int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count) {
+  if (a.nreal <= 0) return RG_OK;
+  if (a.M <= 16) return launch_sweep_t<16, 64>(a, stream, sm_count);
+  if (a.M <= 32) return launch_sweep_t<32, 128>(a, stream, sm_count);
+  if (a.M <= kMaxModesSmem) return launch_sweep_t<64, 256>(a, stream, sm_count);
+  return fail(RG_ERR_INVALID_ARG, "nmu > 64 is not supported by the shared-memory sweep kernel");
+}
+
+int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
+                     unsigned long long* d_counts, cudaStream_t stream) {
+  const size_t smem = sizeof(unsigned long long) * (nbins + 1);
+  if (smem > 200 * 1024) return fail(RG_ERR_INVALID_ARG, "too many histogram bins");
+  if (smem > 48 * 1024)
+    RG_CUDA(cudaFuncSetAttribute(histogram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 1024) blocks = 1024;
+  if (blocks < 1) blocks = 1;
+  histogram_kernel<<<(int)blocks, 256, smem, stream>>>(d_samples, n, d_bins, nbins, d_counts);
+  RG_CUDA(cudaGetLastError());
+  return RG_OK;
+}
+
+}  // namespace rg

@@ -1,0 +1,768 @@
+// Host side of the C ABI: the waveguide object (init_waveguide and friends,
+// src/waveguide.f90:81-350), device tables, batching and error handling.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rg_internal.h"
+
+using rg::cplx;
+
+namespace rg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(RG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// xoshiro256 jump-ahead.  The state update of xoshiro256 is linear over
+// GF(2); its characteristic polynomial p(x) (degree 256) is recovered with
+// Berlekamp-Massey from one state bit, and advancing the state by d steps is
+// multiplication by x^d mod p(x), evaluated on the state by Horner's rule.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct State {
+  uint64_t s[4];
+};
+
+inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+inline void step(State& st) {
+  uint64_t* s = st.s;
+  const uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = rotl(s[3], 45);
+}
+
+struct CharPoly {
+  uint64_t w[5];  // bit i = coefficient of x^i, degree 256
+};
+
+CharPoly compute_charpoly() {
+  const int N = 512;
+  State st{{0x9e3779b97f4a7c15ULL, 0xbf58476d1ce4e5b9ULL, 0x94d049bb133111ebULL, 0x2545f4914f6cdd1dULL}};
+  std::vector<int> seq(N);
+  for (int i = 0; i < N; ++i) {
+    seq[i] = (int)(st.s[0] & 1ULL);
+    step(st);
+  }
+  // Berlekamp-Massey over GF(2).
+  std::vector<int> C(N + 1, 0), B(N + 1, 0), T;
+  C[0] = B[0] = 1;
+  int L = 0, m = 1;
+  for (int n = 0; n < N; ++n) {
+    int d = seq[n];
+    for (int i = 1; i <= L; ++i) d ^= C[i] & seq[n - i];
+    if (!d) {
+      ++m;
+    } else if (2 * L <= n) {
+      T = C;
+      for (int i = 0; i + m <= N; ++i) C[i + m] ^= B[i];
+      L = n + 1 - L;
+      B = T;
+      m = 1;
+    } else {
+      for (int i = 0; i + m <= N; ++i) C[i + m] ^= B[i];
+      ++m;
+    }
+  }
+  CharPoly p{};
+  // p(x) = x^L C(1/x)
+  for (int i = 0; i <= L; ++i)
+    if (C[L - i]) p.w[i >> 6] |= 1ULL << (i & 63);
+  if (L != 256) p.w[4] = 0;  // flagged by the self-check below
+  return p;
+}
+
+const CharPoly& charpoly() {
+  static const CharPoly p = compute_charpoly();
+  return p;
+}
+
+// a * b mod p for polynomials of degree < 256.
+void mulmod(const uint64_t a[4], const uint64_t b[4], uint64_t out[4]) {
+  const CharPoly& p = charpoly();
+  uint64_t prod[9] = {0};
+  for (int i = 0; i < 256; ++i) {
+    if (!((a[i >> 6] >> (i & 63)) & 1ULL)) continue;
+    const int ws = i >> 6, bs = i & 63;
+    for (int w = 0; w < 4; ++w) {
+      prod[w + ws] ^= b[w] << bs;
+      if (bs) prod[w + ws + 1] ^= b[w] >> (64 - bs);
+    }
+  }
+  for (int deg = 511; deg >= 256; --deg) {
+    if (!((prod[deg >> 6] >> (deg & 63)) & 1ULL)) continue;
+    const int sh = deg - 256, ws = sh >> 6, bs = sh & 63;
+    for (int w = 0; w < 5; ++w) {
+      prod[w + ws] ^= p.w[w] << bs;
+      if (bs && w + ws + 1 < 9) prod[w + ws + 1] ^= p.w[w] >> (64 - bs);
+    }
+  }
+  for (int w = 0; w < 4; ++w) out[w] = prod[w];
+}
+
+void apply_jump(State& st, const uint64_t poly[4]) {
+  State acc{{0, 0, 0, 0}};
+  for (int i = 0; i < 256; ++i) {
+    if ((poly[i >> 6] >> (i & 63)) & 1ULL)
+      for (int k = 0; k < 4; ++k) acc.s[k] ^= st.s[k];
+    step(st);
+  }
+  st = acc;
+}
+
+// One-time check that jump(d) equals d single steps.
+int rng_selfcheck() {
+  static int result = -1;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    if (charpoly().w[4] != 1ULL) {
+      result = 1;
+      return;
+    }
+    State a{{0x0123456789abcdefULL, 0xfedcba9876543210ULL, 0x0f1e2d3c4b5a6978ULL, 0x8796a5b4c3d2e1f0ULL}};
+    State b = a;
+    uint64_t poly[4];
+    jump_polynomial(12345, poly);
+    apply_jump(a, poly);
+    for (int i = 0; i < 12345; ++i) step(b);
+    result = std::memcmp(a.s, b.s, sizeof a.s) != 0;
+  });
+  return result;
+}
+
+}  // namespace
+
+void jump_polynomial(uint64_t distance, uint64_t out[4]) {
+  uint64_t result[4] = {1, 0, 0, 0};  // x^0
+  uint64_t base[4] = {2, 0, 0, 0};    // x^1
+  while (distance) {
+    if (distance & 1ULL) mulmod(result, base, result);
+    mulmod(base, base, base);
+    distance >>= 1;
+  }
+  std::memcpy(out, result, sizeof result);
+}
+
+}  // namespace rg
+
+// ---------------------------------------------------------------------------
+// The waveguide handle.
+// ---------------------------------------------------------------------------
+struct rg_waveguide {
+  rg_params p{};
+  int nmu = 0, ny = 0, nx = 0, imin = 0, imax = 0, jmin = 0, jmax = 0, neigv = 0, nprop = 0;
+  double kl = 0, kdx = 0, dos = 0, stdu = 0;
+  std::vector<double> xmesh, ymesh, kpmesh;
+  std::vector<cplx> mumesh, bmat, aedge, abulk, sqmu_c, sqmu_r;
+  std::vector<double> costab;    // [ny][2*nmu+1], Dirichlet
+  std::vector<cplx> expfac;      // [ny][nmu], periodic
+  std::vector<uint64_t> jump;    // [ny][4]
+
+  int device = 0, sm_count = 0;
+  cudaStream_t stream = nullptr;
+  double2 *d_bmat = nullptr, *d_aedge = nullptr, *d_abulk = nullptr, *d_sqmu_c = nullptr, *d_sqmu_r = nullptr;
+  double* d_costab = nullptr;
+  double2* d_expfac = nullptr;
+  uint64_t* d_jump = nullptr;
+  int* d_counter = nullptr;
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+// Switches to the handle's device for the duration of a call.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+template <class T>
+int upload(T** dst, const void* src, size_t bytes) {
+  if (bytes == 0) {
+    *dst = nullptr;
+    return RG_OK;
+  }
+  RG_CUDA(cudaMalloc((void**)dst, bytes));
+  RG_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+  return RG_OK;
+}
+
+void free_device(rg_waveguide* w) {
+  cudaFree(w->d_bmat);
+  cudaFree(w->d_aedge);
+  cudaFree(w->d_abulk);
+  cudaFree(w->d_sqmu_c);
+  cudaFree(w->d_sqmu_r);
+  cudaFree(w->d_costab);
+  cudaFree(w->d_expfac);
+  cudaFree(w->d_jump);
+  cudaFree(w->d_counter);
+  cudaFree(w->d_scratch);
+  if (w->stream) cudaStreamDestroy(w->stream);
+  w->d_bmat = w->d_aedge = w->d_abulk = w->d_sqmu_c = w->d_sqmu_r = nullptr;
+  w->d_costab = nullptr;
+  w->d_expfac = nullptr;
+  w->d_jump = nullptr;
+  w->d_counter = nullptr;
+  w->d_scratch = nullptr;
+  w->scratch_bytes = 0;
+  w->stream = nullptr;
+}
+
+// Host tables of init_waveguide, src/waveguide.f90:81-255.
+int build_tables(rg_waveguide* w, const rg_params& p) {
+  const double eps = 2.220446049250313e-16;
+  if (p.wol < eps) return rg::fail(RG_ERR_INVALID_ARG, "Invalid width-to-wavelength ratio.");
+  if (p.aratio < eps) return rg::fail(RG_ERR_INVALID_ARG, "Invalid aspect ratio.");
+  if (p.exfac < 1.0 || p.exfac > 1e4)
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid modal basis extension factor. It must be in [1, 10000].");
+  if (p.nxfree < 0) return rg::fail(RG_ERR_INVALID_ARG, "Invalid number of x points, cannot be negative.");
+  if (p.nxdiso < 1 || p.nxdiso + 2 * p.nxfree < 2)
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid number of x points, need nxdiso >= 1 and nx >= 2.");
+  if (p.dscat < 0.0 || p.dabso < 0.0) return rg::fail(RG_ERR_INVALID_ARG, "Invalid optical depth, cannot be negative.");
+  if (!(p.napera > 0.0 && p.napera <= 1.0))
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid filtering parameter napera (expected in ]0, 1]).");
+  if (!(p.naperb > 0.0 && p.naperb <= 1.0))
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid filtering parameter naperb (expected in ]0, 1]).");
+  if (p.ny < 0) return rg::fail(RG_ERR_INVALID_ARG, "Invalid ny, cannot be negative.");
+
+  w->p = p;
+  w->kl = 2.0 * kPi * p.wol * p.aratio;
+  w->nx = p.nxdiso + 2 * p.nxfree;
+  w->kdx = w->kl / p.nxdiso;
+  w->xmesh.resize(w->nx);
+  for (int i = 1; i <= w->nx; ++i) w->xmesh[i - 1] = p.aratio * (i - 0.5 - p.nxfree) / p.nxdiso;
+
+  if (p.boundtype == RG_BOUND_PERIODIC) {
+    if (std::fmod(p.wol, 1.0) == 0.0)
+      return rg::fail(RG_ERR_INVALID_ARG, "Invalid width wol, cannot be an integer for 'periodic' boundary conditions.");
+    w->nmu = 2 * (int)std::floor(p.exfac * p.wol) + 1;
+    w->imin = w->nmu / 2 + 1 - (int)std::floor(p.naperb * p.wol);
+    w->imax = w->nmu / 2 + 1 + (int)std::floor(p.naperb * p.wol);
+    w->jmin = w->nmu / 2 + 1 - (int)std::floor(p.napera * p.wol);
+    w->jmax = w->nmu / 2 + 1 + (int)std::floor(p.napera * p.wol);
+    w->neigv = 2 * (int)std::floor(std::min(p.napera, p.naperb) * p.wol) + 1;
+    w->nprop = 2 * (int)std::floor(p.wol) + 1;
+  } else if (p.boundtype == RG_BOUND_DIRICHLET) {
+    if (std::fmod(p.wol, 0.5) == 0.0)
+      return rg::fail(RG_ERR_INVALID_ARG,
+                      "Invalid width wol, cannot be a half integer for 'dirichlet' boundary conditions.");
+    w->nmu = (int)std::floor(2 * p.exfac * p.wol);
+    w->imin = 1;
+    w->imax = (int)std::floor(2 * p.naperb * p.wol);
+    w->jmin = 1;
+    w->jmax = (int)std::floor(2 * p.napera * p.wol);
+    w->neigv = (int)std::floor(2 * std::min(p.napera, p.naperb) * p.wol);
+    w->nprop = (int)std::floor(2 * p.wol);
+  } else {
+    return rg::fail(RG_ERR_INVALID_ARG, "Unknown boundary condition type.");
+  }
+  const int M = w->nmu;
+  if (M < 1 || w->neigv < 1) return rg::fail(RG_ERR_INVALID_ARG, "Waveguide has no modes (wol too small).");
+  w->ny = p.ny > 0 ? p.ny : M;
+  const int ny = w->ny;
+  w->ymesh.resize(ny);
+  for (int i = 1; i <= ny; ++i) w->ymesh[i - 1] = (i - 0.5) / ny;
+  w->kpmesh.resize(M);
+  if (p.boundtype == RG_BOUND_PERIODIC)
+    for (int n = 1; n <= M; ++n) w->kpmesh[n - 1] = (n - M / 2 - 1) / p.wol;
+  else
+    for (int n = 1; n <= M; ++n) w->kpmesh[n - 1] = 0.5 * n / p.wol;
+
+  // mumesh, dos, bmat and the A diagonals: src/waveguide.f90:240-248,357-363.
+  w->mumesh.resize(M);
+  w->bmat.resize(M);
+  w->aedge.resize(M);
+  w->abulk.resize(M);
+  w->sqmu_c.resize(M);
+  w->sqmu_r.resize(M);
+  double dos = 0.0;
+  for (int n = 0; n < M; ++n) {
+    const double kp = w->kpmesh[n];
+    w->mumesh[n] = std::sqrt(cplx(1.0 - kp * kp, p.dabso / w->kl));
+    dos += std::real(1.0 / std::sqrt(cplx(1.0 - kp * kp, 0.0)));
+  }
+  w->dos = dos / (p.wol * (2.0 * kPi) * (2.0 * kPi));
+  const cplx iu(0.0, 1.0);
+  for (int n = 0; n < M; ++n) {
+    const cplx mu = w->mumesh[n];
+    w->bmat[n] = mu / std::sin(mu * w->kdx);
+    const cplx cot = mu / std::tan(mu * w->kdx);
+    w->aedge[n] = iu * mu - cot;
+    w->abulk[n] = -2.0 * cot;
+    w->sqmu_c[n] = std::sqrt(mu);                              // src/waveguide.f90:443
+    w->sqmu_r[n] = cplx(std::sqrt(std::real(mu)), 0.0);       // src/waveguide.f90:510
+  }
+  w->stdu = std::sqrt(p.dscat * ny / (2.0 * kPi * kPi * w->dos * p.wol * p.nxdiso));  // src/waveguide.f90:370
+
+  // Projection tables.  Dirichlet modes chi_m(y) = sqrt(2/ny) sin(pi m y)
+  // give (modal^T diag(U) modal)[a][c] = cc[|a-c|] - cc[a+c+2] with
+  // cc[d] = sum_j U_j cos(pi d y_j) / ny; periodic modes exp(2 pi i k y)/sqrt(ny)
+  // give the Hermitian Toeplitz f[c-a] with f[d] = sum_j U_j exp(2 pi i d y_j) / ny.
+  if (p.boundtype == RG_BOUND_DIRICHLET) {
+    const int nd = 2 * M + 1;
+    w->costab.resize((size_t)ny * nd);
+    for (int j = 0; j < ny; ++j)
+      for (int d = 0; d < nd; ++d) w->costab[(size_t)j * nd + d] = std::cos(kPi * d * w->ymesh[j]) / ny;
+  } else {
+    w->expfac.resize((size_t)ny * M);
+    for (int j = 0; j < ny; ++j)
+      for (int d = 0; d < M; ++d)
+        w->expfac[(size_t)j * M + d] = cplx(std::cos(2 * kPi * d * w->ymesh[j]), std::sin(2 * kPi * d * w->ymesh[j])) / (double)ny;
+  }
+  // Jump polynomials: column iy of the potential starts 2*nxdiso*iy draws in.
+  w->jump.assign((size_t)ny * 4, 0);
+  uint64_t step_poly[4], cur[4] = {1, 0, 0, 0};
+  rg::jump_polynomial(2ULL * (uint64_t)p.nxdiso, step_poly);
+  for (int iy = 0; iy < ny; ++iy) {
+    std::memcpy(&w->jump[(size_t)iy * 4], cur, sizeof cur);
+    rg::mulmod(cur, step_poly, cur);
+  }
+  return RG_OK;
+}
+
+int upload_tables(rg_waveguide* w) {
+  RG_CUDA(cudaGetDevice(&w->device));
+  RG_CUDA(cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->device));
+  RG_CUDA(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+  const size_t cb = sizeof(double2) * w->nmu;
+  int rc;
+  if ((rc = upload(&w->d_bmat, w->bmat.data(), cb))) return rc;
+  if ((rc = upload(&w->d_aedge, w->aedge.data(), cb))) return rc;
+  if ((rc = upload(&w->d_abulk, w->abulk.data(), cb))) return rc;
+  if ((rc = upload(&w->d_sqmu_c, w->sqmu_c.data(), cb))) return rc;
+  if ((rc = upload(&w->d_sqmu_r, w->sqmu_r.data(), cb))) return rc;
+  if ((rc = upload(&w->d_costab, w->costab.data(), sizeof(double) * w->costab.size()))) return rc;
+  if ((rc = upload(&w->d_expfac, w->expfac.data(), sizeof(double2) * w->expfac.size()))) return rc;
+  if ((rc = upload(&w->d_jump, w->jump.data(), sizeof(uint64_t) * w->jump.size()))) return rc;
+  RG_CUDA(cudaMalloc((void**)&w->d_counter, sizeof(int)));
+  return RG_OK;
+}
+
+int ensure_scratch(rg_waveguide* w, size_t bytes) {
+  if (bytes <= w->scratch_bytes) return RG_OK;
+  cudaFree(w->d_scratch);
+  w->d_scratch = nullptr;
+  w->scratch_bytes = 0;
+  cudaError_t e = cudaMalloc(&w->d_scratch, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return rg::fail(RG_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+  }
+  w->scratch_bytes = bytes;
+  return RG_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+rg::SweepArgs base_args(const rg_waveguide* w) {
+  rg::SweepArgs a{};
+  a.M = w->nmu;
+  a.ny = w->ny;
+  a.nx = w->nx;
+  a.nxdiso = w->p.nxdiso;
+  a.nxfree = w->p.nxfree;
+  a.row0 = w->imin - 1;
+  a.nrow = w->imax - w->imin + 1;
+  a.col0 = w->jmin - 1;
+  a.ncol = w->jmax - w->jmin + 1;
+  a.neigv = w->neigv;
+  a.mode = rg::kModeEig;
+  a.bmat = w->d_bmat;
+  a.adiag_edge = w->d_aedge;
+  a.adiag_bulk = w->d_abulk;
+  a.sqmu = w->d_sqmu_c;
+  a.costab = w->d_costab;
+  a.expfac = w->d_expfac;
+  a.periodic = w->p.boundtype == RG_BOUND_PERIODIC;
+  a.work_counter = w->d_counter;
+  return a;
+}
+
+// Largest number of realizations whose potentials are held at once.
+int potential_chunk(const rg_waveguide* w, int n) {
+  const size_t per = sizeof(double) * (size_t)w->p.nxdiso * w->ny;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)8 << 30;
+  size_t budget = std::min((size_t)48 << 30, free_b / 2);
+  long long c = (long long)(budget / std::max<size_t>(per, 1));
+  if (c < 1) c = 1;
+  return (int)std::min<long long>(c, n);
+}
+
+// Seed-driven batch on device buffers: potentials are drawn chunk by chunk
+// into scratch, then swept.  d_seeds, d_teig, d_status are device pointers.
+int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_teig, int32_t* d_status,
+                   cudaStream_t s) {
+  const int chunk = potential_chunk(w, n);
+  const size_t pot_bytes = sizeof(double) * (size_t)w->p.nxdiso * w->ny * chunk;
+  int rc = ensure_scratch(w, align256(pot_bytes));
+  if (rc) return rc;
+  double* d_pot = (double*)w->d_scratch;
+  for (int k0 = 0; k0 < n; k0 += chunk) {
+    const int nk = std::min(chunk, n - k0);
+    rg::PotArgs pa{};
+    pa.nxdiso = w->p.nxdiso;
+    pa.ny = w->ny;
+    pa.nreal = nk;
+    pa.stdu = w->stdu;
+    pa.seeds = d_seeds + k0;
+    pa.jumppoly = w->d_jump;
+    pa.upot = d_pot;
+    if ((rc = rg::launch_potential(pa, s))) return rc;
+    rg::SweepArgs a = base_args(w);
+    a.nreal = nk;
+    a.upot = d_pot;
+    a.pot_rstride = (int64_t)w->p.nxdiso * w->ny;
+    a.pot_xstride = w->ny;
+    a.pot_ystride = 1;
+    a.teig = d_teig + (int64_t)k0 * w->neigv;
+    a.status = d_status + k0;
+    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+    if ((rc = rg::launch_sweep(a, s, w->sm_count))) return rc;
+  }
+  return RG_OK;
+}
+
+int first_bad_status(const int32_t* st, int n) {
+  for (int k = 0; k < n; ++k)
+    if (st[k] != RG_OK) return st[k];
+  return RG_OK;
+}
+
+const char* status_text(int code) {
+  switch (code) {
+    case RG_ERR_SINGULAR: return "zgetrf: Matrix is numerically singular (zero or NaN pivot)";
+    case RG_ERR_NOCONV: return "singular values did not converge";
+    default: return "error";
+  }
+}
+
+// Single realization with either a seed or a host potential; mode selects
+// the eigenvalue path (tdistrib) or the full-t path (v1).
+int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int mode, double* h_teig,
+               double* h_t, double* h_tfilt) {
+  DeviceGuard g(w->device);
+  const int M = w->nmu;
+  const size_t pot = sizeof(double) * (size_t)w->p.nxdiso * w->ny;
+  const int nrow = mode == rg::kModeEig ? w->imax - w->imin + 1 : M;
+  const int ncol = mode == rg::kModeEig ? w->jmax - w->jmin + 1 : M;
+  const size_t tbytes = sizeof(double2) * (size_t)nrow * ncol;
+  const size_t off_t = align256(pot), off_e = off_t + align256(tbytes);
+  const size_t off_s = off_e + align256(sizeof(double) * w->neigv), off_seed = off_s + 256;
+  int rc = ensure_scratch(w, off_seed + 256);
+  if (rc) return rc;
+  char* base = (char*)w->d_scratch;
+  double* d_pot = (double*)base;
+  double2* d_t = (double2*)(base + off_t);
+  double* d_teig = (double*)(base + off_e);
+  int32_t* d_status = (int32_t*)(base + off_s);
+  int32_t* d_seed = (int32_t*)(base + off_seed);
+  cudaStream_t s = w->stream;
+  rg::SweepArgs a = base_args(w);
+  a.nreal = 1;
+  a.upot = d_pot;
+  if (seed) {
+    RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    rg::PotArgs pa{};
+    pa.nxdiso = w->p.nxdiso;
+    pa.ny = w->ny;
+    pa.nreal = 1;
+    pa.stdu = w->stdu;
+    pa.seeds = d_seed;
+    pa.jumppoly = w->d_jump;
+    pa.upot = d_pot;
+    if ((rc = rg::launch_potential(pa, s))) return rc;
+    a.pot_rstride = 0;
+    a.pot_xstride = w->ny;
+    a.pot_ystride = 1;
+  } else {
+    // caller layout upot(nxdiso, ny), x fastest
+    RG_CUDA(cudaMemcpyAsync(d_pot, h_upot, pot, cudaMemcpyHostToDevice, s));
+    a.pot_rstride = 0;
+    a.pot_xstride = 1;
+    a.pot_ystride = w->p.nxdiso;
+  }
+  a.mode = mode;
+  if (mode == rg::kModeTmat) {
+    a.row0 = 0;
+    a.nrow = M;
+    a.col0 = 0;
+    a.ncol = M;
+    a.sqmu = w->d_sqmu_r;
+  }
+  a.tout = (h_t || h_tfilt) ? d_t : nullptr;
+  a.teig = d_teig;
+  a.status = d_status;
+  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  if ((rc = rg::launch_sweep(a, s, w->sm_count))) return rc;
+  int32_t st = 0;
+  RG_CUDA(cudaMemcpyAsync(&st, d_status, sizeof st, cudaMemcpyDeviceToHost, s));
+  if (h_teig) RG_CUDA(cudaMemcpyAsync(h_teig, d_teig, sizeof(double) * w->neigv, cudaMemcpyDeviceToHost, s));
+  if (h_t) RG_CUDA(cudaMemcpyAsync(h_t, d_t, tbytes, cudaMemcpyDeviceToHost, s));
+  if (h_tfilt) RG_CUDA(cudaMemcpyAsync(h_tfilt, d_t, tbytes, cudaMemcpyDeviceToHost, s));
+  RG_CUDA(cudaStreamSynchronize(s));
+  if (st != RG_OK) return rg::fail(st, status_text(st));
+  return RG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* rg_last_error(void) { return rg::g_last_error.c_str(); }
+
+int rg_init(const rg_params* params, rg_waveguide** out) {
+  if (!params || !out) return rg::fail(RG_ERR_INVALID_ARG, "rg_init: NULL argument");
+  *out = nullptr;
+  if (rg::rng_selfcheck() != 0) return rg::fail(RG_ERR_INVALID_ARG, "xoshiro256 jump-ahead self-check failed");
+  rg_waveguide* w = new (std::nothrow) rg_waveguide();
+  if (!w) return rg::fail(RG_ERR_NOMEM, "rg_init: out of host memory");
+  int rc = build_tables(w, *params);
+  if (!rc) rc = upload_tables(w);
+  if (rc) {
+    free_device(w);
+    delete w;
+    return rc;
+  }
+  *out = w;
+  return RG_OK;
+}
+
+int rg_init_copy(const rg_waveguide* src, rg_waveguide** out) {
+  if (!src) return rg::fail(RG_ERR_INVALID_ARG, "rg_init_copy: NULL source");
+  DeviceGuard g(src->device);
+  return rg_init(&src->p, out);
+}
+
+void rg_del(rg_waveguide* w) {
+  if (!w) return;
+  {
+    DeviceGuard g(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    free_device(w);
+  }
+  delete w;
+}
+
+int rg_get_nmu(const rg_waveguide* w) { return w ? w->nmu : -1; }
+int rg_get_neigv(const rg_waveguide* w) { return w ? w->neigv : -1; }
+int rg_get_nx(const rg_waveguide* w) { return w ? w->nx : -1; }
+int rg_get_ny(const rg_waveguide* w) { return w ? w->ny : -1; }
+int rg_get_nprop(const rg_waveguide* w) { return w ? w->nprop : -1; }
+
+int rg_get_window(const rg_waveguide* w, int* imin, int* imax, int* jmin, int* jmax) {
+  if (!w || !imin || !imax || !jmin || !jmax) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_window: NULL argument");
+  *imin = w->imin;
+  *imax = w->imax;
+  *jmin = w->jmin;
+  *jmax = w->jmax;
+  return RG_OK;
+}
+
+int rg_get_xmesh(const rg_waveguide* w, double* xmesh, int64_t len) {
+  if (!w || !xmesh) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_xmesh: NULL argument");
+  if (len != w->nx) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_xmesh: length must equal nx");
+  std::memcpy(xmesh, w->xmesh.data(), sizeof(double) * w->nx);
+  return RG_OK;
+}
+
+int rg_get_parameters(const rg_waveguide* w, rg_params* out) {
+  if (!w || !out) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_parameters: NULL argument");
+  *out = w->p;
+  return RG_OK;
+}
+
+int rg_get_scalars(const rg_waveguide* w, double* kdx, double* dos, double* stdu) {
+  if (!w) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_scalars: NULL handle");
+  if (kdx) *kdx = w->kdx;
+  if (dos) *dos = w->dos;
+  if (stdu) *stdu = w->stdu;
+  return RG_OK;
+}
+
+int rg_compute_tdistrib(rg_waveguide* w, int iseed, double* tallvals, int64_t len) {
+  if (!w || !tallvals) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_tdistrib: NULL argument");
+  // Chunk checks of src/waveguide.f90:408-421.
+  const int64_t nchunk = len / w->neigv;
+  if (nchunk == 0)
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid eigenvalue array length, received " + std::to_string(len) +
+                                            ", expected at least " + std::to_string(w->neigv) + "...");
+  if (nchunk * w->neigv != len)
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid eigenvalue array length, received " + std::to_string(len) +
+                                            ", expected " + std::to_string(nchunk * w->neigv) + "...");
+  if (iseed < 1 || nchunk < iseed)
+    return rg::fail(RG_ERR_INVALID_ARG, "Invalid chunk index, received " + std::to_string(iseed) +
+                                            ", expected in [1, " + std::to_string(nchunk) + "]...");
+  const int32_t s = iseed;
+  return run_single(w, &s, nullptr, rg::kModeEig, tallvals + (iseed - 1) * (int64_t)w->neigv, nullptr, nullptr);
+}
+
+int rg_tdistrib_upot(rg_waveguide* w, const double* upot, double* teigvals, double* tfilt) {
+  if (!w || !upot || !teigvals) return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_upot: NULL argument");
+  return run_single(w, nullptr, upot, rg::kModeEig, teigvals, nullptr, tfilt);
+}
+
+int rg_compute_refl_trans_v1(rg_waveguide* w, int iseed, double* rmat, double* tmat) {
+  if (!w || !tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v1: NULL argument");
+  if (rmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v1: r is not available yet (pass NULL)");
+  const int32_t s = iseed;
+  return run_single(w, &s, nullptr, rg::kModeTmat, nullptr, tmat, nullptr);
+}
+
+int rg_refl_trans_v1_upot(rg_waveguide* w, const double* upot, double* rmat, double* tmat) {
+  if (!w || !upot || !tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_upot: NULL argument");
+  if (rmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_upot: r is not available yet (pass NULL)");
+  return run_single(w, nullptr, upot, rg::kModeTmat, nullptr, tmat, nullptr);
+}
+
+int rg_potential(rg_waveguide* w, int iseed, double* upot) {
+  if (!w || !upot) return rg::fail(RG_ERR_INVALID_ARG, "rg_potential: NULL argument");
+  DeviceGuard g(w->device);
+  const size_t n = (size_t)w->p.nxdiso * w->ny;
+  int rc = ensure_scratch(w, align256(sizeof(double) * n) + 256);
+  if (rc) return rc;
+  double* d_pot = (double*)w->d_scratch;
+  int32_t* d_seed = (int32_t*)((char*)w->d_scratch + align256(sizeof(double) * n));
+  const int32_t s = iseed;
+  RG_CUDA(cudaMemcpyAsync(d_seed, &s, sizeof s, cudaMemcpyHostToDevice, w->stream));
+  rg::PotArgs pa{};
+  pa.nxdiso = w->p.nxdiso;
+  pa.ny = w->ny;
+  pa.nreal = 1;
+  pa.stdu = w->stdu;
+  pa.seeds = d_seed;
+  pa.jumppoly = w->d_jump;
+  pa.upot = d_pot;
+  if ((rc = rg::launch_potential(pa, w->stream))) return rc;
+  std::vector<double> tmp(n);
+  RG_CUDA(cudaMemcpyAsync(tmp.data(), d_pot, sizeof(double) * n, cudaMemcpyDeviceToHost, w->stream));
+  RG_CUDA(cudaStreamSynchronize(w->stream));
+  const int nxd = w->p.nxdiso, ny = w->ny;
+  for (int ix = 0; ix < nxd; ++ix)
+    for (int iy = 0; iy < ny; ++iy) upot[ix + (size_t)nxd * iy] = tmp[(size_t)ix * ny + iy];
+  return RG_OK;
+}
+
+int rg_tdistrib_batch_device(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tallvals, int32_t* d_status,
+                             void* stream) {
+  if (!w || !d_seeds || !d_tallvals || !d_status || n < 0)
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_batch_device: invalid argument");
+  DeviceGuard g(w->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : w->stream;
+  int rc = run_seed_batch(w, d_seeds, n, d_tallvals, d_status, s);
+  if (rc) return rc;
+  RG_CUDA(cudaStreamSynchronize(s));
+  return RG_OK;
+}
+
+int rg_tdistrib_batch(rg_waveguide* w, const int32_t* seeds, int n, double* tallvals, int32_t* status) {
+  if (!w || (n > 0 && (!seeds || !tallvals)) || n < 0)
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_batch: invalid argument");
+  if (n == 0) return RG_OK;
+  DeviceGuard g(w->device);
+  int32_t* d_seeds = nullptr;
+  int32_t* d_status = nullptr;
+  double* d_out = nullptr;
+  const size_t ob = sizeof(double) * (size_t)n * w->neigv;
+  RG_CUDA(cudaMalloc((void**)&d_seeds, sizeof(int32_t) * n));
+  cudaError_t e1 = cudaMalloc((void**)&d_status, sizeof(int32_t) * n);
+  cudaError_t e2 = cudaMalloc((void**)&d_out, ob);
+  int rc = RG_OK;
+  std::vector<int32_t> st_host;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    cudaGetLastError();
+    rc = rg::fail(RG_ERR_NOMEM, "rg_tdistrib_batch: device allocation failed");
+  }
+  cudaStream_t s = w->stream;
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(d_seeds, seeds, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = rg::cuda_fail(e, "copy seeds");
+  }
+  if (!rc) rc = run_seed_batch(w, d_seeds, n, d_out, d_status, s);
+  if (!rc) {
+    st_host.resize(n);
+    cudaError_t e = cudaMemcpyAsync(tallvals, d_out, ob, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st_host.data(), d_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_batch");
+  }
+  cudaFree(d_seeds);
+  cudaFree(d_status);
+  cudaFree(d_out);
+  if (rc) return rc;
+  if (status) std::memcpy(status, st_host.data(), sizeof(int32_t) * n);
+  const int bad = first_bad_status(st_host.data(), n);
+  if (bad) return rg::fail(bad, status_text(bad));
+  return RG_OK;
+}
+
+int rg_histogram(const double* samples, int64_t n, const double* bins, int nbins, double* histo, double* missing) {
+  if (!bins || !histo || !missing || (n > 0 && !samples) || n < 0)
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_histogram: invalid argument");
+  if (nbins < 1) return rg::fail(RG_ERR_INVALID_ARG, "Invalid number of bins");
+  for (int j = 1; j <= nbins; ++j)  // check_histogram, src/base_utils.f90:478-486
+    if (bins[j - 1] > bins[j]) return rg::fail(RG_ERR_INVALID_ARG, "Unsorted array of bins, aborting...");
+  double* d_x = nullptr;
+  double* d_b = nullptr;
+  unsigned long long* d_c = nullptr;
+  const size_t xb = sizeof(double) * (size_t)std::max<int64_t>(n, 1);
+  RG_CUDA(cudaMalloc((void**)&d_x, xb));
+  cudaError_t e = cudaMalloc((void**)&d_b, sizeof(double) * (nbins + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_c, sizeof(unsigned long long) * (nbins + 1));
+  int rc = RG_OK;
+  std::vector<unsigned long long> counts(nbins + 1, 0ULL);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(d_x, samples, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_b, bins, sizeof(double) * (nbins + 1), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(d_c, 0, sizeof(unsigned long long) * (nbins + 1));
+  if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_histogram setup");
+  if (!rc && n > 0) rc = rg::launch_histogram(d_x, n, d_b, nbins, d_c, 0);
+  if (!rc) {
+    e = cudaMemcpy(counts.data(), d_c, sizeof(unsigned long long) * (nbins + 1), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_histogram result");
+  }
+  cudaFree(d_x);
+  cudaFree(d_b);
+  cudaFree(d_c);
+  if (rc) return rc;
+  for (int j = 0; j < nbins; ++j) histo[j] = (double)counts[j];
+  *missing = (double)counts[nbins];
+  return RG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Bars (tolerances stated here, from the project's parity contract):
+  * t: relative Frobenius error <= 1e-10
+  * T_n: absolute error <= 1e-9
+  * histogram counts: identical (edges and comparisons are the reference's)
+Both sides receive the same potential: the oracle's host-drawn upot is passed
+to rg_tdistrib_upot; for seed-driven calls the GPU's own potential is first
+checked against the oracle's.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+import recurgreen_gb300 as rg
+
+pytestmark = pytest.mark.gpu
+
+T_REL = 1e-10
+TN_ABS = 1e-9
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+CASES = {
+    # the reference's own test waveguide (src/waveguide.test.f90:62-73)
+    "ref_test": dict(boundtype="dirichlet", nxdiso=100, nxfree=20, wol=4.30, exfac=1.2, aratio=1.0, dscat=0.2),
+    # the small plain-method config: kW/pi = 10.5 (M = 10), 200 slices, 64 y points, L/l_s = 5
+    "small_c1": dict(boundtype="dirichlet", nxdiso=200, nxfree=0, wol=5.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=64),
+    # ragged Fisher-Lee window (napera < naperb) and absorption
+    "ragged_abs": dict(boundtype="dirichlet", nxdiso=60, nxfree=3, wol=7.3, exfac=1.1, aratio=1.5, dscat=3.0,
+                       dabso=0.5, napera=0.6, naperb=1.0, ny=40),
+    "periodic": dict(boundtype="periodic", nxdiso=80, nxfree=0, wol=6.3, exfac=1.0, aratio=1.0, dscat=2.0),
+    # M = 32 and M = 64 kernels (the 64-mode kernel at the uniform config's width, shorter guide)
+    "m32": dict(boundtype="dirichlet", nxdiso=150, nxfree=0, wol=16.25, exfac=1.0, aratio=1.0, dscat=4.0, ny=128),
+    "m64": dict(boundtype="dirichlet", nxdiso=200, nxfree=0, wol=32.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=256),
+    # the smallest guide: two slices, one mode
+    "tiny": dict(boundtype="dirichlet", nxdiso=2, nxfree=0, wol=0.7, exfac=1.0, aratio=1.0, dscat=1.0),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def pair(request):
+    kw = CASES[request.param]
+    return request.param, O.Waveguide(**kw), rg.Waveguide(**kw)
+
+
+def test_init_matches_oracle(pair):
+    name, o, g = pair
+    assert (g.nmu, g.ny, g.nx, g.neigv, g.nprop) == (o.nmu, o.ny, o.nx, o.neigv, o.nprop)
+    assert (g.imin, g.imax, g.jmin, g.jmax) == (o.imin, o.imax, o.jmin, o.jmax)
+    assert g.kdx == o.kdx and g.dos == o.dos and g.stdu == o.stdu
+
+
+def test_potential_matches_oracle(pair):
+    name, o, g = pair
+    for seed in (1, 17):
+        uo, ug = o.potential(seed), g.potential(seed)
+        # same stream; log/cos of the device libm may differ by a few ulp
+        assert np.max(np.abs(ug - uo)) <= 1e-14 * np.max(np.abs(uo))
+
+
+def test_tdistrib_upot_parity(pair):
+    name, o, g = pair
+    for seed in (1, 2, 3):
+        u = o.potential(seed)
+        To, to = o.tdistrib_upot(u, want_t=True)
+        Tg, tg = g.tdistrib_upot(u, want_t=True)
+        assert relerr(tg, to) <= T_REL, name
+        assert np.max(np.abs(Tg - To)) <= TN_ABS, name
+        assert np.all(np.diff(Tg) <= 0)  # descending, like zgesvd
+
+
+def test_compute_tdistrib_seed_and_chunks(pair):
+    name, o, g = pair
+    nchunk = 3
+    tall = np.zeros(nchunk * g.neigv)
+    g.compute_tdistrib(2, tall)
+    ref = o.tdistrib_upot(o.potential(2))
+    assert np.all(tall[: g.neigv] == 0) and np.all(tall[2 * g.neigv:] == 0)
+    assert np.max(np.abs(tall[g.neigv: 2 * g.neigv] - ref)) <= TN_ABS
+
+
+def test_refl_trans_v1_t(pair):
+    name, o, g = pair
+    u = o.potential(4)
+    ro, to = o.refl_trans_v1_upot(u)
+    tg = g.refl_trans_v1_upot(u)
+    assert relerr(tg, to) <= T_REL
+
+
+def test_batch_equals_single_and_oracle():
+    kw = CASES["small_c1"]
+    g, o = rg.Waveguide(**kw), O.Waveguide(**kw)
+    seeds = np.arange(1, 41, dtype=np.int32)
+    b = g.tdistrib_batch(seeds)
+    ob = o.tdistrib_batch(seeds)
+    assert np.max(np.abs(b - ob)) <= TN_ABS
+    one = np.zeros(g.neigv * 40)
+    g.compute_tdistrib(7, one)
+    np.testing.assert_array_equal(one[6 * g.neigv: 7 * g.neigv], b[6 * g.neigv: 7 * g.neigv])
+
+
+def test_uniform_full_length_two_seeds():
+    """The uniform config's full slice matrix size and length (M=64, ny=256, Nx=2000)."""
+    kw = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=32.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=256)
+    g, o = rg.Waveguide(**kw), O.Waveguide(**kw)
+    for seed in (1, 4096):
+        u = o.potential(seed)
+        To, to = o.tdistrib_upot(u, want_t=True)
+        Tg, tg = g.tdistrib_upot(u, want_t=True)
+        assert relerr(tg, to) <= T_REL
+        assert np.max(np.abs(Tg - To)) <= TN_ABS
+        assert np.all((Tg >= -1e-12) & (Tg <= 1 + 1e-12))  # dabso = 0: 0 <= T <= 1
+
+
+def test_histogram_matches_oracle():
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-0.05, 1.05, 200_000)
+    bins = O.chebyshev_bins(100)
+    x[:6] = [bins[0], bins[-1], bins[37], np.nan, np.nextafter(1.0, 2.0), -0.0]
+    hg, mg = rg.histogram(x, bins)
+    ho, mo = O.histogram(x, bins)
+    np.testing.assert_array_equal(hg, ho)
+    assert mg == mo
+    assert hg.sum() + mg == x.size - 1  # the NaN is dropped
+
+
+def test_errors_are_statuses_not_crashes():
+    with pytest.raises(rg.RecurGreenError) as e:
+        rg.Waveguide("dirichlet", wol=2.5)
+    assert e.value.code == rg.RG_ERR_INVALID_ARG
+    with pytest.raises(rg.RecurGreenError):
+        rg.Waveguide("neumann", wol=2.3)
+    g = rg.Waveguide(**CASES["small_c1"])
+    with pytest.raises(rg.RecurGreenError) as e:
+        g.compute_tdistrib(4, np.zeros(3 * g.neigv))
+    assert "chunk" in str(e.value)
+    with pytest.raises(rg.RecurGreenError):
+        g.compute_tdistrib(1, np.zeros(g.neigv + 1))
+    # a NaN in the potential makes every pivot invalid: singular status, context intact
+    u = g.potential(1)
+    u[:, 0] = np.nan
+    with pytest.raises(rg.RecurGreenError) as e:
+        g.tdistrib_upot(u)
+    assert e.value.code == rg.RG_ERR_SINGULAR
+    T = g.tdistrib_upot(g.potential(1))
+    assert np.all(np.isfinite(T))
