@@ -46,9 +46,10 @@ def flops_per_realization(M: int, nx: int) -> float:
 
 
 def config(batch: int) -> dict:
-    return {"workload": "batched-uniform: M=64 modes (kW/pi=64.5), Nx=2000, ny=256, L/l_s=10, eps=0, "
+    nx = WORKLOAD["nxdiso"]
+    return {"workload": f"batched-uniform: M=64 modes (kW/pi=64.5), Nx={nx}, ny=256, L/l_s=10, eps=0, "
                         f"{batch} realizations (seeds 1..{batch})",
-            "modes": 64, "nx": 2000, "ny": 256, "realizations_per_step": batch,
+            "modes": 64, "nx": nx, "ny": 256, "realizations_per_step": batch,
             "l2": "working set (potentials) 16.8 GB >> L2; no flush needed"}
 
 
@@ -173,7 +174,10 @@ def main() -> None:
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nx", type=int, default=WORKLOAD["nxdiso"],
+                    help="slices (profiling runs only; the workload is Nx=2000)")
     args = ap.parse_args()
+    WORKLOAD["nxdiso"] = args.nx
     if args.impl == "reference":
         run_reference(args)
         return

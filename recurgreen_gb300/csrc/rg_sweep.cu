@@ -113,39 +113,57 @@ __global__ void potential_kernel(PotArgs a) {
 // Sweep kernel
 // ---------------------------------------------------------------------------
 //
-// Shared memory holds the augmented matrix [W | R] (M x 2M complex, row
-// stride LD = 2*MCAP + 1 to spread banks).  W is the slice matrix being
-// inverted in place by Gauss-Jordan; R is the right-hand side B*Gs1, which
-// turns into the new propagator column Gs1 during the same elimination.
+// One realization per CTA; persistent CTAs take realizations from a work
+// counter.  Per slice the kernel solves X Y = R for the slice matrix
+// X = A_n - V_n - B Gss B and the right-hand side R = B Gs1 by Gauss-Jordan
+// elimination, which leaves inv(X) = Gss in W and Y in R, so the new
+// propagator is Gs1 = -Y.
 //
-// Pivoting is implicit: rows are never swapped.  Step k picks, among rows
-// not yet used, the one with the largest |re|+|im| in column k (the izamax
-// rule of zgetrf), scales it, and eliminates column k from every other row.
-// After M steps row piv[a] of R holds row a of inv(X) * R, and W holds
-// inv(X) with rows and columns permuted.  The next slice keeps each R row in
-// place: physical row q of the next augmented matrix carries logical row
-// pinv[q], so R is only rescaled, and W is rebuilt by a row-local gather.
+// W (M x M complex) lives in shared memory (row stride LDW = MCAP + 1);
+// R (M x M complex) lives in registers: thread (warp w, lane l) owns
+// rows w + NW*a and columns l + 32*b.  Keeping R out of shared memory halves
+// the footprint so two realizations share an SM, and the serial phases of
+// one (pivot search, reciprocal, slice assembly) overlap the other's FP64
+// elimination work.
+//
+// Pivoting is implicit: rows are never swapped.  Step k takes, among rows
+// not yet used, the largest max(|re|, |im|) in column k (compared as integer
+// bit patterns, so the search costs no FP64 instructions), scales that row
+// and eliminates column k from every other row.  After M steps row piv[a] of
+// R holds row a of Y, and W holds inv(X) with permuted rows and columns.  The
+// next slice keeps every R row in place: physical row q then carries logical
+// row pinv[q], so R is only rescaled by B, and W is rebuilt by a gather that
+// stays inside each row.
 template <int MCAP, int NT>
 struct SweepSmem {
-  static constexpr int LD = 2 * MCAP + 1;
+  static constexpr int LDW = MCAP + 1;
   static size_t bytes(int ny) {
     const int nyp = (ny + 1) & ~1;
-    return sizeof(double2) * ((size_t)MCAP * LD + MCAP + 2 * MCAP) + sizeof(double) * (2 * MCAP + 2 + nyp) +
+    return sizeof(double2) * ((size_t)MCAP * LDW + 3 * MCAP) + sizeof(double) * (2 * MCAP + 2 + nyp) +
            sizeof(int) * 5 * MCAP;
   }
 };
 
-template <int MCAP, int NT>
-__global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
+__device__ __forceinline__ unsigned long long pivot_key(double2 x) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(x.x) & 0x7fffffffffffffffULL;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x.y) & 0x7fffffffffffffffULL;
+  const unsigned long long m = a > b ? a : b;
+  return m > 0x7ff0000000000000ULL ? 0ULL : m;  // NaN never wins
+}
+
+template <int MCAP, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
   constexpr int NW = NT / 32;
-  constexpr int LD = SweepSmem<MCAP, NT>::LD;
+  constexpr int LDW = SweepSmem<MCAP, NT>::LDW;
   constexpr int AMAX = (MCAP + NW - 1) / NW;  // rows per warp
-  constexpr int BMAX = (2 * MCAP + 31) / 32;  // augmented columns per lane
+  constexpr int CB = (MCAP + 31) / 32;        // column blocks per lane
+  constexpr int TMAX = (MCAP * MCAP + NT - 1) / NT;
   extern __shared__ double2 smem[];
-  double2* aug = smem;                         // [MCAP][LD]
-  double2* colbuf = aug + MCAP * LD;           // [MCAP]   column k before the update
-  double2* rowbuf = colbuf + MCAP;             // [2*MCAP] scaled pivot row
-  double* cc = (double*)(rowbuf + 2 * MCAP);   // [2*MCAP+2] projection coefficients
+  double2* W = smem;                           // [MCAP][LDW]
+  double2* colbuf = W + MCAP * LDW;            // [MCAP] column k before the update
+  double2* rowW = colbuf + MCAP;               // [MCAP] scaled pivot row of W
+  double2* rowR = rowW + MCAP;                 // [MCAP] scaled pivot row of R
+  double* cc = (double*)(rowR + MCAP);         // [2*MCAP+2] projection coefficients
   double* urow = cc + (2 * MCAP + 2);          // [ny] potential of the slice
   int* piv = (int*)(urow + ((a.ny + 1) & ~1)); // [MCAP] pivot row of column k
   int* pinv = piv + MCAP;                      // [MCAP] column of which row q was pivot
@@ -156,7 +174,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
   __shared__ double2 s_d;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int M = a.M, M2 = 2 * a.M;
+  const int M = a.M;
+  double2 R[AMAX][CB];
 
   for (;;) {
     if (tid == 0) s_r = atomicAdd(a.work_counter, 1);
@@ -168,6 +187,11 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
       sinv[c] = c;
       used[c] = 0;
     }
+#pragma unroll
+    for (int ai = 0; ai < AMAX; ++ai)
+#pragma unroll
+      for (int b = 0; b < CB; ++b)
+        R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? 1.0 : 0.0, 0.0);
     const double* U = a.upot + (int64_t)r * a.pot_rstride;
     __syncthreads();
 
@@ -181,7 +205,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
         if (!a.periodic) {
           // cc[d] = (1/ny) sum_j U_j cos(pi d y_j), d = 0..2M, so that
           // (modal^T diag(U) modal)[a][c] = cc[|a-c|] - cc[a+c+2].
-          const int nd = M2 + 1;
+          const int nd = 2 * M + 1;
           for (int d = tid; d < nd; d += NT) {
             const double* ct = a.costab + d;
             double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
@@ -213,75 +237,69 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
         __syncthreads();
       }
 
-      // 2. Assemble X = A_n - V_n - B Gss B in physical row order, and the
-      //    right-hand side R = B Gs1 (identity on the first slice).
+      // 2. Assemble X = A_n - V_n - B Gss B in physical row order (W), and
+      //    R = B Gs1 (identity on the first slice; registers, in place).
       const double2* adiag = (n == 0 || n == a.nx - 1) ? a.adiag_edge : a.adiag_bulk;
-      const double rsign = (n == 1) ? 1.0 : -1.0;  // Gs1 = +Gss after slice 1, -Gss B Gs1 after
+      const double rsign = (n == 1) ? 1.0 : -1.0;  // Gs1 = +Y after slice 1, -Y after later slices
+#pragma unroll
       for (int ai = 0; ai < AMAX; ++ai) {
         const int q = warp + NW * ai;
-        if (q >= M) break;
-        const int al = (n == 0) ? q : pinv[q];  // logical row carried by physical row q
-        const double2 ba = a.bmat[al];
-        double2 v[BMAX];
+        if (q < M) {
+          const int al = (n == 0) ? q : pinv[q];  // logical row carried by physical row q
+          const double2 ba = a.bmat[al];
+          double2 v[CB];
 #pragma unroll
-        for (int b = 0; b < BMAX; ++b) {
-          const int J = lane + 32 * b;
-          double2 x = make_double2(0.0, 0.0);
-          if (J < M) {
-            const int c = J;
-            if (al == c) x = adiag[c];
-            if (dis) {
-              double2 vac;
-              if (!a.periodic) {
-                const int dd = al > c ? al - c : c - al;
-                vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
-              } else {
-                vac = (c >= al) ? make_double2(cc[2 * (c - al)], cc[2 * (c - al) + 1])
-                                : make_double2(cc[2 * (al - c)], -cc[2 * (al - c) + 1]);
+          for (int b = 0; b < CB; ++b) {
+            const int c = lane + 32 * b;
+            double2 x = make_double2(0.0, 0.0);
+            if (c < M) {
+              if (al == c) x = adiag[c];
+              if (dis) {
+                double2 vac;
+                if (!a.periodic) {
+                  const int dd = al > c ? al - c : c - al;
+                  vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
+                } else {
+                  vac = (c >= al) ? make_double2(cc[2 * (c - al)], cc[2 * (c - al) + 1])
+                                  : make_double2(cc[2 * (al - c)], -cc[2 * (al - c) + 1]);
+                }
+                x = csub(x, vac);
               }
-              x = csub(x, vac);
+              if (n > 0) x = csub(x, cmul(cmul(ba, W[q * LDW + colmap[c]]), a.bmat[c]));
+              if (n > 0) R[ai][b] = cmul(ba, cscale(rsign, R[ai][b]));
             }
-            if (n > 0) {
-              const double2 g = aug[q * LD + colmap[c]];
-              x = csub(x, cmul(cmul(ba, g), a.bmat[c]));
-            }
-          } else if (J < M2) {
-            if (n == 0) {
-              x = make_double2(J - M == q ? 1.0 : 0.0, 0.0);
-            } else {
-              x = cmul(ba, cscale(rsign, aug[q * LD + J]));
-            }
+            v[b] = x;
           }
-          v[b] = x;
-        }
-        __syncwarp();
+          __syncwarp();
 #pragma unroll
-        for (int b = 0; b < BMAX; ++b) {
-          const int J = lane + 32 * b;
-          if (J < M2) aug[q * LD + J] = v[b];
+          for (int b = 0; b < CB; ++b) {
+            const int c = lane + 32 * b;
+            if (c < M) W[q * LDW + c] = v[b];
+          }
         }
       }
       __syncthreads();
 
-      // 3. Gauss-Jordan elimination with implicit partial pivoting.
+      // 3. Gauss-Jordan elimination, three barriers per step:
+      //    A: warp 0 finds the pivot row p of column k and d = 1/X[p][k];
+      //    B: the scaled pivot rows of W and R go to shared memory;
+      //    C: every thread updates its W and R elements.
       for (int k = 0; k < M; ++k) {
         if (warp == 0) {
-          double best = -1.0;
+          unsigned long long best = 0ULL;
           int bi = 0x7fffffff;
           for (int i = lane; i < M; i += 32) {
-            const double2 x = aug[i * LD + k];
+            const double2 x = W[i * LDW + k];
             colbuf[i] = x;
-            if (!used[i]) {
-              const double m = fabs(x.x) + fabs(x.y);
-              if (m > best) {
-                best = m;
-                bi = i;
-              }
+            const unsigned long long key = used[i] ? 0ULL : pivot_key(x);
+            if (key > best) {
+              best = key;
+              bi = i;
             }
           }
 #pragma unroll
           for (int off = 16; off; off >>= 1) {
-            const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
             const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
             if (ob > best || (ob == best && oi < bi)) {
               best = ob;
@@ -290,16 +308,14 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
           }
           if (lane == 0) {
             double2 d = make_double2(0.0, 0.0);
-            if (!(best > 0.0)) {  // zero or NaN column: numerically singular
+            if (best == 0ULL) {  // zero or NaN column: numerically singular
               s_status = RG_ERR_SINGULAR;
-              if (bi >= M) {
-                bi = 0;
-                while (bi < M - 1 && used[bi]) ++bi;
-              }
+              bi = 0;
+              while (bi < M - 1 && used[bi]) ++bi;
             } else {
               const double2 z = colbuf[bi];
-              const double den = z.x * z.x + z.y * z.y;
-              d = make_double2(z.x / den, -z.y / den);
+              const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
+              d = make_double2(z.x * rden, -z.y * rden);
             }
             used[bi] = 1;
             piv[k] = bi;
@@ -311,33 +327,45 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
         __syncthreads();
         const int p = s_p;
         const double2 d = s_d;
-        for (int J = tid; J < M2; J += NT) rowbuf[J] = (J == k) ? d : cmul(aug[p * LD + J], d);
-        __syncthreads();
-        double2 rv[BMAX];
+        for (int J = tid; J < M; J += NT) rowW[J] = (J == k) ? d : cmul(W[p * LDW + J], d);
+        if (warp == p % NW) {
+          const int ap = p / NW;
 #pragma unroll
-        for (int b = 0; b < BMAX; ++b) {
-          const int J = lane + 32 * b;
-          rv[b] = (J < M2) ? rowbuf[J] : make_double2(0.0, 0.0);
+          for (int b = 0; b < CB; ++b) {
+            const int j = lane + 32 * b;
+            double2 val = R[0][b];
+#pragma unroll
+            for (int ai = 1; ai < AMAX; ++ai)
+              if (ai == ap) val = R[ai][b];
+            if (j < M) rowR[j] = cmul(val, d);
+          }
         }
+        __syncthreads();
+        double2 rw[CB], rr[CB];
+#pragma unroll
+        for (int b = 0; b < CB; ++b) {
+          const int J = lane + 32 * b;
+          rw[b] = (J < M) ? rowW[J] : make_double2(0.0, 0.0);
+          rr[b] = (J < M) ? rowR[J] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
         for (int ai = 0; ai < AMAX; ++ai) {
           const int i = warp + NW * ai;
-          if (i >= M) break;
-          double2* row = aug + i * LD;
-          if (i == p) {
-#pragma unroll
-            for (int b = 0; b < BMAX; ++b) {
-              const int J = lane + 32 * b;
-              if (J < M2) row[J] = rv[b];
-            }
-          } else {
+          if (i < M) {
             const double2 f = colbuf[i];
+            const bool isp = (i == p);
+            double2 wv[CB];
 #pragma unroll
-            for (int b = 0; b < BMAX; ++b) {
+            for (int b = 0; b < CB; ++b) {
               const int J = lane + 32 * b;
-              if (J < M2) {
-                const double2 w = (J == k) ? make_double2(0.0, 0.0) : row[J];
-                row[J] = cfms(w, f, rv[b]);
-              }
+              wv[b] = (J < M && J != k) ? W[i * LDW + J] : make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int b = 0; b < CB; ++b) {
+              const int J = lane + 32 * b;
+              wv[b] = isp ? rw[b] : cfms(wv[b], f, rw[b]);
+              R[ai][b] = isp ? rr[b] : cfms(R[ai][b], f, rr[b]);
+              if (J < M) W[i * LDW + J] = wv[b];
             }
           }
         }
@@ -355,29 +383,52 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
     }
 
     // 5. Fisher-Lee: Gs1[a][j] = sign * R[piv[a]][j]; t = 2i sqmu_a Gs1 sqmu_j.
+    //    R goes to shared memory (physical rows), t is formed in registers
+    //    and then stored over it for the eigenvalue stage.
+#pragma unroll
+    for (int ai = 0; ai < AMAX; ++ai) {
+      const int q = warp + NW * ai;
+#pragma unroll
+      for (int b = 0; b < CB; ++b) {
+        const int j = lane + 32 * b;
+        if (q < M && j < M) W[q * LDW + j] = R[ai][b];
+      }
+    }
+    __syncthreads();
     const double gsign = (a.nx >= 2) ? -1.0 : 1.0;
     const int nrow = a.nrow, ncol = a.ncol;
     double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
-    for (int e = tid; e < nrow * ncol; e += NT) {
-      const int i = e % nrow, j = e / nrow;
-      const int gi = a.row0 + i, gj = a.col0 + j;
-      const double2 g = cscale(gsign, aug[piv[gi] * LD + M + gj]);
-      const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
-      const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);  // (0, 2) * v
-      if (tout) tout[e] = t;
-      if (a.mode == kModeEig) aug[i * LD + j] = t;
+    double2 tv[TMAX];
+#pragma unroll
+    for (int s = 0; s < TMAX; ++s) {
+      const int e = tid + NT * s;
+      tv[s] = make_double2(0.0, 0.0);
+      if (e < nrow * ncol) {
+        const int i = e % nrow, j = e / nrow;
+        const int gi = a.row0 + i, gj = a.col0 + j;
+        const double2 g = cscale(gsign, W[piv[gi] * LDW + gj]);
+        const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
+        tv[s] = make_double2(-2.0 * v.y, 2.0 * v.x);  // (0, 2) * v
+        if (tout) tout[e] = tv[s];
+      }
     }
     __syncthreads();
 
     if (a.mode == kModeEig) {
+#pragma unroll
+      for (int s = 0; s < TMAX; ++s) {
+        const int e = tid + NT * s;
+        if (e < nrow * ncol) W[(e % nrow) * LDW + e / nrow] = tv[s];
+      }
+      __syncthreads();
       // 6. Eigenvalues of t^H t by one-sided (Hestenes) Jacobi on the
       //    vectors of the smaller dimension: columns of t if nrow >= ncol,
       //    else rows (the singular values of t^T equal those of t).
       const bool bycol = nrow >= ncol;
       const int nv = bycol ? ncol : nrow;
       const int L = bycol ? nrow : ncol;
-      const int es = bycol ? LD : 1;  // element stride inside a vector
-      const int vs = bycol ? 1 : LD;  // stride between vectors
+      const int es = bycol ? LDW : 1;  // element stride inside a vector
+      const int vs = bycol ? 1 : LDW;  // stride between vectors
       const int NP = (nv + 1) & ~1;
       const double tol = 2.220446049250313e-16 * L;
       int sweep = 0;
@@ -390,8 +441,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
             const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
             const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
             if (vp >= nv || vq >= nv) continue;
-            double2* xp = aug + vp * vs;
-            double2* xq = aug + vq * vs;
+            double2* xp = W + vp * vs;
+            double2* xq = W + vq * vs;
             double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
             for (int i = lane; i < L; i += 32) {
               const double2 u = xp[i * es], w = xq[i * es];
@@ -431,7 +482,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(SweepArgs a) {
       if (sweep == 60 && tid == 0) s_status = RG_ERR_NOCONV;
       // T_k = |v_k|^2, sorted descending into teig.
       for (int k = warp; k < nv; k += NW) {
-        const double2* xk = aug + k * vs;
+        const double2* xk = W + k * vs;
         double s = 0.0;
         for (int i = lane; i < L; i += 32) {
           const double2 u = xk[i * es];
@@ -487,16 +538,16 @@ __global__ void histogram_kernel(const double* __restrict__ x, int64_t n, const 
     if (hs[i]) atomicAdd(&counts[i], hs[i]);
 }
 
-template <int MCAP, int NT>
+template <int MCAP, int NT, int MINB>
 int launch_sweep_t(const SweepArgs& a, cudaStream_t stream, int sm_count) {
   const size_t smem = SweepSmem<MCAP, NT>::bytes(a.ny);
-  RG_CUDA(cudaFuncSetAttribute(sweep_kernel<MCAP, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RG_CUDA(cudaFuncSetAttribute(sweep_kernel<MCAP, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<MCAP, NT>, NT, smem));
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<MCAP, NT, MINB>, NT, smem));
   if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "sweep kernel does not fit on an SM (ny too large?)");
   int grid = per_sm * sm_count;
   if (grid > a.nreal) grid = a.nreal;
-  sweep_kernel<MCAP, NT><<<grid, NT, smem, stream>>>(a);
+  sweep_kernel<MCAP, NT, MINB><<<grid, NT, smem, stream>>>(a);
   RG_CUDA(cudaGetLastError());
   return RG_OK;
 }
@@ -513,9 +564,9 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
 
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count) {
   if (a.nreal <= 0) return RG_OK;
-  if (a.M <= 16) return launch_sweep_t<16, 64>(a, stream, sm_count);
-  if (a.M <= 32) return launch_sweep_t<32, 128>(a, stream, sm_count);
-  if (a.M <= kMaxModesSmem) return launch_sweep_t<64, 256>(a, stream, sm_count);
+  if (a.M <= 16) return launch_sweep_t<16, 64, 8>(a, stream, sm_count);
+  if (a.M <= 32) return launch_sweep_t<32, 128, 4>(a, stream, sm_count);
+  if (a.M <= kMaxModesSmem) return launch_sweep_t<64, 256, 2>(a, stream, sm_count);
   return fail(RG_ERR_INVALID_ARG, "nmu > 64 is not supported by the shared-memory sweep kernel");
 }
 
