@@ -127,6 +127,21 @@ int rg_tdistrib_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* tal
 int rg_tdistrib_batch_device(rg_waveguide* wg, const int32_t* d_seeds, int n, double* d_tallvals,
                              int32_t* d_status, void* stream);
 
+/* No counterpart in the reference.  One seed's transmission eigenvalues, as
+ * rg_compute_tdistrib computes them, for callers that cannot allocate device
+ * memory when they need the result: code running during CUDA stream capture,
+ * hosts whose device memory is handed to their own pool, and loops that must
+ * not take cudaMalloc's implicit synchronisation.  The call allocates nothing:
+ * create the handle with rg_init at set-up, then call this with device
+ * buffers d_teigvals[neigv] and d_status[1]; work is enqueued on `stream`
+ * (NULL: the handle's stream) and the call returns without synchronising.
+ * The potential is drawn into a fixed 16 MiB device array of the library,
+ * shared by all calls, so nxdiso*ny may be at most 2,097,120; larger guides
+ * get RG_ERR_INVALID_ARG.  The handle's device must be current; the first
+ * call on each device looks the array up (make it before any stream capture).
+ * Calls that overlap on the GPU race on the shared array. */
+int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_teigvals, int32_t* d_status, void* stream);
+
 /* histogram (src/base_utils.f90:491-516) with the reference's exact edge
  * semantics, computed on the GPU: samples[n] and bins[nbins+1] are host
  * arrays; histo[nbins] and *missing receive counts as doubles. */

@@ -76,4 +76,15 @@ int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, i
 // xoshiro256** jump-ahead polynomials (rg_waveguide.cpp).
 void jump_polynomial(uint64_t distance, uint64_t out[4]);
 
+// Read-only view of a handle for the allocation-free entry point
+// (rg_noalloc.cu): sizes, device tables and the base sweep arguments.
+struct NoAllocView {
+  int device, sm_count, nxdiso, ny;
+  double stdu;
+  const uint64_t* jumppoly;
+  cudaStream_t stream;
+  SweepArgs sweep;
+};
+int noalloc_view(const rg_waveguide* w, NoAllocView* out);
+
 }  // namespace rg

@@ -540,6 +540,23 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
 
 }  // namespace
 
+namespace rg {
+
+int noalloc_view(const rg_waveguide* w, NoAllocView* out) {
+  if (!w || !out) return fail(RG_ERR_INVALID_ARG, "noalloc_view: NULL argument");
+  out->device = w->device;
+  out->sm_count = w->sm_count;
+  out->nxdiso = w->p.nxdiso;
+  out->ny = w->ny;
+  out->stdu = w->stdu;
+  out->jumppoly = w->d_jump;
+  out->stream = w->stream;
+  out->sweep = base_args(w);
+  return RG_OK;
+}
+
+}  // namespace rg
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
