@@ -127,6 +127,13 @@ int rg_tdistrib_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* tal
 int rg_tdistrib_batch_device(rg_waveguide* wg, const int32_t* d_seeds, int n, double* d_tallvals,
                              int32_t* d_status, void* stream);
 
+/* Tracing (the reference times its seed loop with date_and_time,
+ * src/main.f90:145,174-176): device time in milliseconds of the sweep kernel
+ * launched by the last rg_tdistrib_batch[_device] call on this handle,
+ * measured with CUDA events recorded around that launch on its stream.
+ * Fails if the last batch needed more than one sweep launch. */
+int rg_last_sweep_time(rg_waveguide* wg, float* ms);
+
 /* No counterpart in the reference.  One seed's transmission eigenvalues, as
  * rg_compute_tdistrib computes them, for callers that cannot allocate device
  * memory when they need the result: code running during CUDA stream capture,

@@ -26,7 +26,7 @@ EXPORTS = (
     "rg_get_ny", "rg_get_nprop", "rg_get_window", "rg_get_xmesh", "rg_get_parameters", "rg_get_scalars",
     "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
-    "rg_tdistrib_seed_noalloc",
+    "rg_tdistrib_seed_noalloc", "rg_last_sweep_time",
 )
 
 
@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
     L.rg_tdistrib_batch_device.argtypes = [vp, vp, C.c_int, vp, vp, vp]
     L.rg_histogram.argtypes = [dp, i64, dp, C.c_int, dp, dp]
     L.rg_tdistrib_seed_noalloc.argtypes = [vp, C.c_int, vp, vp, vp]
+    L.rg_last_sweep_time.argtypes = [vp, C.POINTER(C.c_float)]
     _LIB = L
     return L
 

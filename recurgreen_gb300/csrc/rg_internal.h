@@ -53,6 +53,12 @@ struct SweepArgs {
   double2* tout;              // [nreal * nrow * ncol] column-major t (optional)
   int32_t* status;            // [nreal]
   int* work_counter;          // persistent-scheduling counter, zeroed before launch
+  // Large-mode kernel (M > kMaxModesSmem) only:
+  const int32_t* seeds;       // [nreal] seeds; the potential is drawn in-kernel when upot == nullptr
+  const uint64_t* jumppoly;   // [ny * 4] jump polynomials for the in-kernel draw
+  double stdu;                // potential standard deviation for the in-kernel draw
+  double2* work;              // per-CTA workspace in global memory
+  int64_t work_stride;        // double2 elements per CTA
 };
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
@@ -70,6 +76,9 @@ struct PotArgs {
 // Launchers (rg_sweep.cu).  All enqueue on `stream`.
 int launch_potential(const PotArgs& a, cudaStream_t stream);
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count);
+// Large-mode sweep (rg_sweep_large.cu): grid size and workspace it needs, and the launch.
+int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
                      unsigned long long* d_counts, cudaStream_t stream);
 

@@ -20,63 +20,10 @@
 // whole chip) is the roofline of the sweep; shared memory, registers and HBM
 // have ample headroom, so the kernel keeps each slice matrix resident in
 // shared memory and spends its FP64 operations only on the elimination.
-#include "rg_internal.h"
+#include "rg_device.cuh"
 
 namespace rg {
 namespace {
-
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
-}
-// w - f * r with four FMAs.
-__device__ __forceinline__ double2 cfms(double2 w, double2 f, double2 r) {
-  return make_double2(fma(-f.x, r.x, fma(f.y, r.y, w.x)), fma(-f.x, r.y, fma(-f.y, r.x, w.y)));
-}
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
-
-// ---------------------------------------------------------------------------
-// Disorder generator
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
-
-struct Xoshiro {
-  uint64_t s0, s1, s2, s3;
-  __device__ __forceinline__ void step() {
-    const uint64_t t = s1 << 17;
-    s2 ^= s0;
-    s3 ^= s1;
-    s1 ^= s2;
-    s0 ^= s3;
-    s2 ^= t;
-    s3 = rotl64(s3, 45);
-  }
-  __device__ __forceinline__ uint64_t next() {
-    const uint64_t r = rotl64(s1 * 5, 7) * 9;
-    step();
-    return r;
-  }
-};
-
-// Seed array of random_seed(put=) from the ANSI-C LCG (randi_ansic,
-// src/random_normal.f90:20-31), scrambled into the 256-bit state the way
-// gfortran's runtime does it (last put element first, XOR keys).
-__device__ Xoshiro seeded_state(int32_t seed) {
-  uint32_t s = (uint32_t)seed, put[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    s = 1103515245u * s + 12345u;
-    put[i] = s;
-  }
-  const uint64_t k0 = 0xbd0c5b6e50c2df49ULL, k1 = 0xd46061cd46e1df38ULL;
-  const uint64_t k2 = 0xbb4f4d4ed6103544ULL, k3 = 0x114a583d0756ad39ULL;
-  Xoshiro x;
-  x.s0 = ((uint64_t)put[7] | ((uint64_t)put[6] << 32)) ^ k0;
-  x.s1 = ((uint64_t)put[5] | ((uint64_t)put[4] << 32)) ^ k1;
-  x.s2 = ((uint64_t)put[3] | ((uint64_t)put[2] << 32)) ^ k2;
-  x.s3 = ((uint64_t)put[1] | ((uint64_t)put[0] << 32)) ^ k3;
-  return x;
-}
 
 // Thread (iy, r): column iy of realization r.  The reference stream is
 // upot(ix, iy) = normal[ix + iy * nxdiso] (reshape, src/waveguide.f90:372),
@@ -87,26 +34,9 @@ __global__ void potential_kernel(PotArgs a) {
   const int iy = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
   if (iy >= a.ny || r >= a.nreal) return;
-  Xoshiro st = seeded_state(a.seeds[r]);
-  const uint64_t* poly = a.jumppoly + 4 * (int64_t)iy;
-  Xoshiro acc{0, 0, 0, 0};
-  for (int w = 0; w < 4; ++w) {
-    const uint64_t pw = poly[w];
-    for (int b = 0; b < 64; ++b) {
-      if ((pw >> b) & 1ULL) {
-        acc.s0 ^= st.s0; acc.s1 ^= st.s1; acc.s2 ^= st.s2; acc.s3 ^= st.s3;
-      }
-      st.step();
-    }
-  }
-  st = acc;
-  const double twopi = 2.0 * 3.141592653589793;
+  Xoshiro st = jump_state(seeded_state(a.seeds[r]), a.jumppoly + 4 * (int64_t)iy);
   double* out = a.upot + (int64_t)r * a.nxdiso * a.ny + iy;
-  for (int ix = 0; ix < a.nxdiso; ++ix) {
-    const double u1 = (double)(st.next() >> 11) * 0x1.0p-53;
-    const double u2 = (double)(st.next() >> 11) * 0x1.0p-53;
-    out[(int64_t)ix * a.ny] = a.stdu * (sqrt(-2.0 * log(u1)) * cos(twopi * u2));
-  }
+  for (int ix = 0; ix < a.nxdiso; ++ix) out[(int64_t)ix * a.ny] = scaled_normal(a.stdu, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -143,13 +73,6 @@ struct SweepSmem {
            sizeof(int) * 5 * MCAP;
   }
 };
-
-__device__ __forceinline__ unsigned long long pivot_key(double2 x) {
-  const unsigned long long a = (unsigned long long)__double_as_longlong(x.x) & 0x7fffffffffffffffULL;
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x.y) & 0x7fffffffffffffffULL;
-  const unsigned long long m = a > b ? a : b;
-  return m > 0x7ff0000000000000ULL ? 0ULL : m;  // NaN never wins
-}
 
 template <int MCAP, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
@@ -567,7 +490,7 @@ int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count) {
   if (a.M <= 16) return launch_sweep_t<16, 64, 8>(a, stream, sm_count);
   if (a.M <= 32) return launch_sweep_t<32, 128, 4>(a, stream, sm_count);
   if (a.M <= kMaxModesSmem) return launch_sweep_t<64, 256, 2>(a, stream, sm_count);
-  return fail(RG_ERR_INVALID_ARG, "nmu > 64 is not supported by the shared-memory sweep kernel");
+  return fail(RG_ERR_INVALID_ARG, "nmu > 64 goes through the large-mode kernel");
 }
 
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,

@@ -1,0 +1,454 @@
+// Recursive Green sweep for many modes (M > 64): the slice matrices no longer
+// fit in shared memory, so W (the slice matrix inverted in place) and R (the
+// propagator right-hand side) live in a per-CTA workspace in global memory
+// (L2-resident when the batch allows), and Gauss-Jordan runs blocked:
+//
+//   for each panel of NB columns
+//     load the panel (M x NB) into shared memory,
+//     factor it: NB pivoted elimination steps restricted to the panel,
+//       recording the multipliers u_k (x <- x + u_k x[p_k] is step k),
+//     apply the NB steps to every other column at once:
+//       z = (I - L)^-1 x[p_0..p_NB-1]  (L[k][l] = u_l[p_k], l < k),
+//       x += U z                       (a rank-NB update, one column per thread),
+//     store the panel back.
+//
+// Same mathematics as the shared-memory kernel (src/waveguide.f90:426-445:
+// Gss = inv(A - B Gss B), Gs1 = -Gss B Gs1, Fisher-Lee), with the same implicit
+// pivoting and permutation bookkeeping; each matrix element is read and
+// written once per panel instead of once per step, so memory traffic is
+// 1/NB of the unblocked elimination.  The disorder is drawn in-kernel, one
+// xoshiro256** state per transverse column kept in the workspace, so the
+// Nx x ny potential of a large guide never goes through HBM.
+#include "rg_device.cuh"
+
+namespace rg {
+namespace {
+
+constexpr int kLargeNT = 256;
+constexpr int kLargeNB = 8;
+
+struct LargeSmem {
+  static size_t bytes(int M, int ny) {
+    const int nyp = (ny + 1) & ~1;
+    return sizeof(double2) * (2 * (size_t)M * kLargeNB + kLargeNB * kLargeNB + M + kLargeNB) +
+           sizeof(double) * (2 * M + 2 + nyp) + sizeof(int) * 5 * M;
+  }
+};
+
+// Workspace of one CTA, in double2 units: W (two buffers), R, t, generator states.
+inline int64_t large_stride(int M, int ny) {
+  const int64_t mm = (int64_t)M * M;
+  return ((4 * mm + 2 * (int64_t)ny) + 15) & ~(int64_t)15;
+}
+
+__global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
+  constexpr int NT = kLargeNT, NB = kLargeNB, NW = NT / 32;
+  const int M = a.M, ny = a.ny;
+  const int64_t mm = (int64_t)M * M;
+  extern __shared__ double2 sm[];
+  double2* P = sm;                          // [M][NB] current panel
+  double2* Ub = P + M * NB;                 // [M][NB] multipliers of the panel's steps
+  double2* Lt = Ub + M * NB;                // [NB][NB] Lt[k][l] = u_l[p_k], l < k
+  double2* colf = Lt + NB * NB;             // [M] panel column before the step
+  double2* rowp = colf + M;                 // [NB] scaled pivot row inside the panel
+  double* cc = (double*)(rowp + NB);        // [2M+2] projection coefficients
+  double* urow = cc + (2 * M + 2);          // [ny] potential of the slice
+  int* piv = (int*)(urow + ((ny + 1) & ~1));
+  int* pinv = piv + M;
+  int* sinv = pinv + M;
+  int* colmap = sinv + M;
+  int* used = colmap + M;
+  __shared__ int s_r, s_p, s_status, s_rot;
+  __shared__ double2 s_d;
+  __shared__ unsigned long long s_key[NW];
+  __shared__ int s_idx[NW];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double2* ws = a.work + (int64_t)blockIdx.x * a.work_stride;
+  double2* const Wb0 = ws;
+  double2* const Wb1 = ws + mm;
+  double2* Rg = ws + 2 * mm;
+  double2* Tg = ws + 3 * mm;
+  uint64_t* gen = (uint64_t*)(ws + 4 * mm);  // [ny][4]
+  const bool draw = (a.upot == nullptr);
+
+  for (;;) {
+    if (tid == 0) s_r = atomicAdd(a.work_counter, 1);
+    __syncthreads();
+    const int r = s_r;
+    if (r >= a.nreal) break;
+    if (tid == 0) s_status = RG_OK;
+    for (int c = tid; c < M; c += NT) {
+      sinv[c] = c;
+      used[c] = 0;
+    }
+    for (int64_t e = tid; e < mm; e += NT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    if (draw) {
+      for (int iy = tid; iy < ny; iy += NT) {
+        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), a.jumppoly + 4 * (int64_t)iy);
+        gen[4 * iy + 0] = st.s0;
+        gen[4 * iy + 1] = st.s1;
+        gen[4 * iy + 2] = st.s2;
+        gen[4 * iy + 3] = st.s3;
+      }
+    }
+    const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;
+    __syncthreads();
+
+    int cur = 0;
+    for (int n = 0; n < a.nx; ++n) {
+      const int id = n - a.nxfree;
+      const bool dis = (id >= 0 && id < a.nxdiso);
+      if (dis) {
+        // 1. This slice's potential row (drawn or loaded) and its projection.
+        if (draw) {
+          for (int iy = tid; iy < ny; iy += NT) {
+            Xoshiro st{gen[4 * iy], gen[4 * iy + 1], gen[4 * iy + 2], gen[4 * iy + 3]};
+            urow[iy] = scaled_normal(a.stdu, st);
+            gen[4 * iy + 0] = st.s0;
+            gen[4 * iy + 1] = st.s1;
+            gen[4 * iy + 2] = st.s2;
+            gen[4 * iy + 3] = st.s3;
+          }
+        } else {
+          for (int j = tid; j < ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+        }
+        __syncthreads();
+        if (!a.periodic) {
+          const int nd = 2 * M + 1;
+          for (int d = tid; d < nd; d += NT) {
+            const double* ct = a.costab + d;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int j = 0;
+            for (; j + 4 <= ny; j += 4) {
+              s0 = fma(ct[(int64_t)(j + 0) * nd], urow[j + 0], s0);
+              s1 = fma(ct[(int64_t)(j + 1) * nd], urow[j + 1], s1);
+              s2 = fma(ct[(int64_t)(j + 2) * nd], urow[j + 2], s2);
+              s3 = fma(ct[(int64_t)(j + 3) * nd], urow[j + 3], s3);
+            }
+            for (; j < ny; ++j) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
+            cc[d] = (s0 + s1) + (s2 + s3);
+          }
+        } else {
+          for (int d = tid; d < M; d += NT) {
+            const double2* et = a.expfac + d;
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < ny; ++j) {
+              const double2 e = et[(int64_t)j * M];
+              sr = fma(e.x, urow[j], sr);
+              si = fma(e.y, urow[j], si);
+            }
+            cc[2 * d] = sr;
+            cc[2 * d + 1] = si;
+          }
+        }
+        __syncthreads();
+      }
+
+      // 2. Assemble X = A_n - V_n - B Gss B (physical row order) into the
+      //    other W buffer, and R = B Gs1 in place.
+      double2* Wold = cur ? Wb1 : Wb0;
+      double2* W = cur ? Wb0 : Wb1;
+      cur ^= 1;
+      const double2* adiag = (n == 0 || n == a.nx - 1) ? a.adiag_edge : a.adiag_bulk;
+      const double rsign = (n == 1) ? 1.0 : -1.0;
+      for (int64_t e = tid; e < mm; e += NT) {
+        const int q = (int)(e / M), c = (int)(e % M);
+        const int al = (n == 0) ? q : pinv[q];
+        double2 x = (al == c) ? adiag[c] : make_double2(0.0, 0.0);
+        if (dis) {
+          double2 vac;
+          if (!a.periodic) {
+            const int dd = al > c ? al - c : c - al;
+            vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
+          } else {
+            vac = (c >= al) ? make_double2(cc[2 * (c - al)], cc[2 * (c - al) + 1])
+                            : make_double2(cc[2 * (al - c)], -cc[2 * (al - c) + 1]);
+          }
+          x = csub(x, vac);
+        }
+        if (n > 0) {
+          x = csub(x, cmul(cmul(a.bmat[al], Wold[(int64_t)q * M + colmap[c]]), a.bmat[c]));
+          Rg[e] = cmul(a.bmat[al], cscale(rsign, Rg[e]));
+        }
+        W[e] = x;
+      }
+      __syncthreads();
+
+      // 3. Blocked Gauss-Jordan with implicit partial pivoting.
+      for (int k0 = 0; k0 < M; k0 += NB) {
+        const int nbk = min(NB, M - k0);
+        for (int e = tid; e < M * nbk; e += NT) {
+          const int i = e / nbk, l = e % nbk;
+          P[i * NB + l] = W[(int64_t)i * M + k0 + l];
+        }
+        __syncthreads();
+        for (int kk = 0; kk < nbk; ++kk) {
+          // a. pivot: largest max(|re|,|im|) among unused rows (ties: lowest row)
+          unsigned long long best = 0ULL;
+          int bi = 0x7fffffff;
+          for (int i = tid; i < M; i += NT) {
+            const unsigned long long key = used[i] ? 0ULL : pivot_key(P[i * NB + kk]);
+            if (key > best) {
+              best = key;
+              bi = i;
+            }
+          }
+#pragma unroll
+          for (int off = 16; off; off >>= 1) {
+            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) {
+              best = ob;
+              bi = oi;
+            }
+          }
+          if (lane == 0) {
+            s_key[warp] = best;
+            s_idx[warp] = bi;
+          }
+          __syncthreads();
+          if (warp == 0) {
+            best = lane < NW ? s_key[lane] : 0ULL;
+            bi = lane < NW ? s_idx[lane] : 0x7fffffff;
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+              const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+              if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+              }
+            }
+            if (lane == 0) {
+              double2 d = make_double2(0.0, 0.0);
+              if (best == 0ULL) {  // zero or NaN column: numerically singular
+                s_status = RG_ERR_SINGULAR;
+                bi = 0;
+                while (bi < M - 1 && used[bi]) ++bi;
+              } else {
+                const double2 z = P[bi * NB + kk];
+                const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
+                d = make_double2(z.x * rden, -z.y * rden);
+              }
+              used[bi] = 1;
+              piv[k0 + kk] = bi;
+              pinv[bi] = k0 + kk;
+              s_p = bi;
+              s_d = d;
+            }
+          }
+          __syncthreads();
+          const int p = s_p;
+          const double2 d = s_d;
+          // b. multipliers u_k and the scaled pivot row of the panel
+          for (int i = tid; i < M; i += NT) {
+            const double2 f = P[i * NB + kk];
+            colf[i] = f;
+            const double2 fd = cmul(f, d);
+            Ub[i * NB + kk] = (i == p) ? make_double2(d.x - 1.0, d.y) : make_double2(-fd.x, -fd.y);
+          }
+          if (tid < nbk) rowp[tid] = (tid == kk) ? d : cmul(P[p * NB + tid], d);
+          __syncthreads();
+          // c. eliminate inside the panel
+          for (int e = tid; e < M * nbk; e += NT) {
+            const int i = e / nbk, l = e % nbk;
+            if (i == p) {
+              P[i * NB + l] = rowp[l];
+            } else {
+              const double2 w = (l == kk) ? make_double2(0.0, 0.0) : P[i * NB + l];
+              P[i * NB + l] = cfms(w, colf[i], rowp[l]);
+            }
+          }
+          __syncthreads();
+        }
+        for (int e = tid; e < nbk * nbk; e += NT) {
+          const int k = e / nbk, l = e % nbk;
+          Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
+        }
+        __syncthreads();
+        // d. the panel's steps applied to every other column of [W | R]
+        const int ntrail = 2 * M - nbk;
+        for (int jj = tid; jj < ntrail; jj += NT) {
+          const int j = jj < k0 ? jj : jj + nbk;
+          double2* col = (j < M) ? W + j : Rg + (j - M);
+          double2 z[NB];
+#pragma unroll
+          for (int k = 0; k < NB; ++k) {
+            z[k] = make_double2(0.0, 0.0);
+            if (k < nbk) {
+              double2 v = col[(int64_t)piv[k0 + k] * M];
+#pragma unroll
+              for (int l = 0; l < k; ++l) v = cfms(v, make_double2(-Lt[k * NB + l].x, -Lt[k * NB + l].y), z[l]);
+              z[k] = v;
+            }
+          }
+          if (nbk == NB) {
+            for (int i = 0; i < M; ++i) {
+              double2 x = col[(int64_t)i * M];
+              const double2* ui = Ub + i * NB;
+#pragma unroll
+              for (int k = 0; k < NB; ++k) {
+                const double2 u = ui[k];
+                x = cfms(x, make_double2(-u.x, -u.y), z[k]);
+              }
+              col[(int64_t)i * M] = x;
+            }
+          } else {
+            for (int i = 0; i < M; ++i) {
+              double2 x = col[(int64_t)i * M];
+              const double2* ui = Ub + i * NB;
+              for (int k = 0; k < nbk; ++k) {
+                const double2 u = ui[k];
+                x = cfms(x, make_double2(-u.x, -u.y), z[k]);
+              }
+              col[(int64_t)i * M] = x;
+            }
+          }
+        }
+        __syncthreads();
+        for (int e = tid; e < M * nbk; e += NT) {
+          const int i = e / nbk, l = e % nbk;
+          W[(int64_t)i * M + k0 + l] = P[i * NB + l];
+        }
+        __syncthreads();
+      }
+
+      // 4. Permutation bookkeeping for the next slice.
+      for (int c = tid; c < M; c += NT) {
+        const int cm = pinv[sinv[c]];
+        sinv[c] = piv[c];
+        colmap[c] = cm;
+        used[c] = 0;
+      }
+      __syncthreads();
+    }
+
+    // 5. Fisher-Lee: t = 2i sqmu_a Gs1 sqmu_j with Gs1[a][j] = sign * R[piv[a]][j];
+    //    t goes to the workspace, column-major (ld = nrow).
+    const double gsign = (a.nx >= 2) ? -1.0 : 1.0;
+    const int nrow = a.nrow, ncol = a.ncol;
+    double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
+    for (int e = tid; e < nrow * ncol; e += NT) {
+      const int i = e % nrow, j = e / nrow;
+      const int gi = a.row0 + i, gj = a.col0 + j;
+      const double2 g = cscale(gsign, Rg[(int64_t)piv[gi] * M + gj]);
+      const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
+      const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);
+      Tg[e] = t;
+      if (tout) tout[e] = t;
+    }
+    __syncthreads();
+
+    if (a.mode == kModeEig) {
+      // 6. Eigenvalues of t^H t: one-sided Jacobi on the vectors of the
+      //    smaller dimension (columns of t, or its rows), in the workspace.
+      const bool bycol = nrow >= ncol;
+      const int nv = bycol ? ncol : nrow;
+      const int L = bycol ? nrow : ncol;
+      const int es = bycol ? 1 : nrow;
+      const int vs = bycol ? nrow : 1;
+      const int NP = (nv + 1) & ~1;
+      const double tol = 2.220446049250313e-16 * L;
+      int sweep = 0;
+      for (; sweep < 60; ++sweep) {
+        if (tid == 0) s_rot = 0;
+        __syncthreads();
+        for (int rr = 0; rr < NP - 1; ++rr) {
+          for (int pk = warp; pk < NP / 2; pk += NW) {
+            const int pos1 = pk, pos2 = NP - 1 - pk;
+            const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
+            const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
+            if (vp >= nv || vq >= nv) continue;
+            double2* xp = Tg + (int64_t)vp * vs;
+            double2* xq = Tg + (int64_t)vq * vs;
+            double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+            for (int i = lane; i < L; i += 32) {
+              const double2 u = xp[(int64_t)i * es], w = xq[(int64_t)i * es];
+              al = fma(u.x, u.x, fma(u.y, u.y, al));
+              be = fma(w.x, w.x, fma(w.y, w.y, be));
+              gr = fma(u.x, w.x, fma(u.y, w.y, gr));
+              gi = fma(u.x, w.y, fma(-u.y, w.x, gi));
+            }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              al += __shfl_xor_sync(0xffffffffu, al, off);
+              be += __shfl_xor_sync(0xffffffffu, be, off);
+              gr += __shfl_xor_sync(0xffffffffu, gr, off);
+              gi += __shfl_xor_sync(0xffffffffu, gi, off);
+            }
+            const double ga = sqrt(gr * gr + gi * gi);
+            if (ga > tol * sqrt(al * be) && ga > 1e-300) {
+              if (lane == 0) s_rot = 1;
+              const double zeta = (be - al) / (2.0 * ga);
+              const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
+                                                  : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+              const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+              const double2 ph = make_double2(gr / ga, -gi / ga);
+              for (int i = lane; i < L; i += 32) {
+                const double2 u = xp[(int64_t)i * es];
+                const double2 w = cmul(ph, xq[(int64_t)i * es]);
+                xp[(int64_t)i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
+                xq[(int64_t)i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
+              }
+            }
+          }
+          __syncthreads();
+        }
+        if (!s_rot) break;
+        __syncthreads();
+      }
+      if (sweep == 60 && tid == 0) s_status = RG_ERR_NOCONV;
+      for (int k = warp; k < nv; k += NW) {
+        const double2* xk = Tg + (int64_t)k * vs;
+        double s = 0.0;
+        for (int i = lane; i < L; i += 32) {
+          const double2 u = xk[(int64_t)i * es];
+          s = fma(u.x, u.x, fma(u.y, u.y, s));
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) cc[k] = s;
+      }
+      __syncthreads();
+      for (int k = tid; k < nv; k += NT) {
+        const double tk = cc[k];
+        int rank = 0;
+        for (int j = 0; j < nv; ++j) {
+          const double tj = cc[j];
+          rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+        }
+        if (rank < a.neigv) a.teig[(int64_t)r * a.neigv + rank] = tk;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) a.status[r] = s_status;
+  }
+}
+
+}  // namespace
+
+int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+  const size_t smem = LargeSmem::bytes(a.M, a.ny);
+  if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes or transverse points for the large-mode kernel");
+  RG_CUDA(cudaFuncSetAttribute(sweep_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_large_kernel, kLargeNT, smem));
+  if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "large-mode sweep kernel does not fit on an SM");
+  int g = per_sm * sm_count;
+  if (g > a.nreal) g = a.nreal;
+  if (g < 1) g = 1;
+  *grid = g;
+  *work_stride = large_stride(a.M, a.ny);
+  return RG_OK;
+}
+
+int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid) {
+  if (a.nreal <= 0) return RG_OK;
+  const size_t smem = LargeSmem::bytes(a.M, a.ny);
+  sweep_large_kernel<<<grid, kLargeNT, smem, stream>>>(a);
+  RG_CUDA(cudaGetLastError());
+  return RG_OK;
+}
+
+}  // namespace rg

@@ -189,6 +189,8 @@ struct rg_waveguide {
   int* d_counter = nullptr;
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
+  cudaEvent_t ev_sweep0 = nullptr, ev_sweep1 = nullptr;  // around the last batch's sweep launches
+  bool sweep_timed = false;
 };
 
 namespace {
@@ -230,6 +232,10 @@ void free_device(rg_waveguide* w) {
   cudaFree(w->d_jump);
   cudaFree(w->d_counter);
   cudaFree(w->d_scratch);
+  if (w->ev_sweep0) cudaEventDestroy(w->ev_sweep0);
+  if (w->ev_sweep1) cudaEventDestroy(w->ev_sweep1);
+  w->ev_sweep0 = w->ev_sweep1 = nullptr;
+  w->sweep_timed = false;
   if (w->stream) cudaStreamDestroy(w->stream);
   w->d_bmat = w->d_aedge = w->d_abulk = w->d_sqmu_c = w->d_sqmu_r = nullptr;
   w->d_costab = nullptr;
@@ -368,6 +374,8 @@ int upload_tables(rg_waveguide* w) {
   if ((rc = upload(&w->d_expfac, w->expfac.data(), sizeof(double2) * w->expfac.size()))) return rc;
   if ((rc = upload(&w->d_jump, w->jump.data(), sizeof(uint64_t) * w->jump.size()))) return rc;
   RG_CUDA(cudaMalloc((void**)&w->d_counter, sizeof(int)));
+  RG_CUDA(cudaEventCreate(&w->ev_sweep0));
+  RG_CUDA(cudaEventCreate(&w->ev_sweep1));
   return RG_OK;
 }
 
@@ -422,13 +430,41 @@ int potential_chunk(const rg_waveguide* w, int n) {
   return (int)std::min<long long>(c, n);
 }
 
-// Seed-driven batch on device buffers: potentials are drawn chunk by chunk
-// into scratch, then swept.  d_seeds, d_teig, d_status are device pointers.
+bool large_modes(const rg_waveguide* w) { return w->nmu > rg::kMaxModesSmem; }
+
+// Seed-driven batch on device buffers.  Up to 64 modes: potentials are drawn
+// chunk by chunk into scratch, then swept.  More modes: one launch of the
+// large-mode kernel, which draws the potential slice by slice itself and
+// needs only its per-CTA workspace.  d_seeds, d_teig, d_status are device
+// pointers.
 int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_teig, int32_t* d_status,
                    cudaStream_t s) {
+  int rc;
+  if (large_modes(w)) {
+    rg::SweepArgs a = base_args(w);
+    a.nreal = n;
+    a.upot = nullptr;
+    a.seeds = d_seeds;
+    a.jumppoly = w->d_jump;
+    a.stdu = w->stdu;
+    a.teig = d_teig;
+    a.status = d_status;
+    int grid = 0;
+    int64_t stride = 0;
+    if ((rc = rg::sweep_large_plan(a, w->sm_count, &grid, &stride))) return rc;
+    if ((rc = ensure_scratch(w, sizeof(double2) * (size_t)stride * grid))) return rc;
+    a.work = (double2*)w->d_scratch;
+    a.work_stride = stride;
+    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+    RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
+    if ((rc = rg::launch_sweep_large(a, s, grid))) return rc;
+    RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
+    w->sweep_timed = true;
+    return RG_OK;
+  }
   const int chunk = potential_chunk(w, n);
   const size_t pot_bytes = sizeof(double) * (size_t)w->p.nxdiso * w->ny * chunk;
-  int rc = ensure_scratch(w, align256(pot_bytes));
+  rc = ensure_scratch(w, align256(pot_bytes));
   if (rc) return rc;
   double* d_pot = (double*)w->d_scratch;
   for (int k0 = 0; k0 < n; k0 += chunk) {
@@ -451,8 +487,11 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
     a.teig = d_teig + (int64_t)k0 * w->neigv;
     a.status = d_status + k0;
     RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+    if (k0 == 0) RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
     if ((rc = rg::launch_sweep(a, s, w->sm_count))) return rc;
   }
+  RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
+  w->sweep_timed = chunk >= n;  // one sweep launch: the events bracket exactly it
   return RG_OK;
 }
 
@@ -471,50 +510,25 @@ const char* status_text(int code) {
 }
 
 // Single realization with either a seed or a host potential; mode selects
-// the eigenvalue path (tdistrib) or the full-t path (v1).
+// the eigenvalue path (tdistrib) or the full-t path (v1).  The scratch is
+// laid out once for the whole call: [potential | t | eigenvalues | status |
+// seed | large-mode workspace].
 int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int mode, double* h_teig,
                double* h_t, double* h_tfilt) {
   DeviceGuard g(w->device);
   const int M = w->nmu;
-  const size_t pot = sizeof(double) * (size_t)w->p.nxdiso * w->ny;
+  const bool large = large_modes(w);
+  const bool draw_in_kernel = large && seed != nullptr;
+  const size_t pot = draw_in_kernel ? 0 : sizeof(double) * (size_t)w->p.nxdiso * w->ny;
   const int nrow = mode == rg::kModeEig ? w->imax - w->imin + 1 : M;
   const int ncol = mode == rg::kModeEig ? w->jmax - w->jmin + 1 : M;
   const size_t tbytes = sizeof(double2) * (size_t)nrow * ncol;
   const size_t off_t = align256(pot), off_e = off_t + align256(tbytes);
   const size_t off_s = off_e + align256(sizeof(double) * w->neigv), off_seed = off_s + 256;
-  int rc = ensure_scratch(w, off_seed + 256);
-  if (rc) return rc;
-  char* base = (char*)w->d_scratch;
-  double* d_pot = (double*)base;
-  double2* d_t = (double2*)(base + off_t);
-  double* d_teig = (double*)(base + off_e);
-  int32_t* d_status = (int32_t*)(base + off_s);
-  int32_t* d_seed = (int32_t*)(base + off_seed);
-  cudaStream_t s = w->stream;
+  const size_t off_ws = off_seed + 256;
+
   rg::SweepArgs a = base_args(w);
   a.nreal = 1;
-  a.upot = d_pot;
-  if (seed) {
-    RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    rg::PotArgs pa{};
-    pa.nxdiso = w->p.nxdiso;
-    pa.ny = w->ny;
-    pa.nreal = 1;
-    pa.stdu = w->stdu;
-    pa.seeds = d_seed;
-    pa.jumppoly = w->d_jump;
-    pa.upot = d_pot;
-    if ((rc = rg::launch_potential(pa, s))) return rc;
-    a.pot_rstride = 0;
-    a.pot_xstride = w->ny;
-    a.pot_ystride = 1;
-  } else {
-    // caller layout upot(nxdiso, ny), x fastest
-    RG_CUDA(cudaMemcpyAsync(d_pot, h_upot, pot, cudaMemcpyHostToDevice, s));
-    a.pot_rstride = 0;
-    a.pot_xstride = 1;
-    a.pot_ystride = w->p.nxdiso;
-  }
   a.mode = mode;
   if (mode == rg::kModeTmat) {
     a.row0 = 0;
@@ -523,11 +537,56 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
     a.ncol = M;
     a.sqmu = w->d_sqmu_r;
   }
+  int grid = 1, rc;
+  int64_t stride = 0;
+  if (large && (rc = rg::sweep_large_plan(a, w->sm_count, &grid, &stride))) return rc;
+  if ((rc = ensure_scratch(w, off_ws + (large ? sizeof(double2) * (size_t)stride * grid : 0)))) return rc;
+  char* base = (char*)w->d_scratch;
+  double* d_pot = (double*)base;
+  double2* d_t = (double2*)(base + off_t);
+  double* d_teig = (double*)(base + off_e);
+  int32_t* d_status = (int32_t*)(base + off_s);
+  int32_t* d_seed = (int32_t*)(base + off_seed);
+  cudaStream_t s = w->stream;
+  a.upot = d_pot;
+  a.pot_rstride = 0;
+  if (seed) {
+    RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    if (draw_in_kernel) {
+      a.upot = nullptr;
+      a.seeds = d_seed;
+      a.jumppoly = w->d_jump;
+      a.stdu = w->stdu;
+    } else {
+      rg::PotArgs pa{};
+      pa.nxdiso = w->p.nxdiso;
+      pa.ny = w->ny;
+      pa.nreal = 1;
+      pa.stdu = w->stdu;
+      pa.seeds = d_seed;
+      pa.jumppoly = w->d_jump;
+      pa.upot = d_pot;
+      if ((rc = rg::launch_potential(pa, s))) return rc;
+      a.pot_xstride = w->ny;
+      a.pot_ystride = 1;
+    }
+  } else {
+    // caller layout upot(nxdiso, ny), x fastest
+    RG_CUDA(cudaMemcpyAsync(d_pot, h_upot, pot, cudaMemcpyHostToDevice, s));
+    a.pot_xstride = 1;
+    a.pot_ystride = w->p.nxdiso;
+  }
   a.tout = (h_t || h_tfilt) ? d_t : nullptr;
   a.teig = d_teig;
   a.status = d_status;
   RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
-  if ((rc = rg::launch_sweep(a, s, w->sm_count))) return rc;
+  if (large) {
+    a.work = (double2*)(base + off_ws);
+    a.work_stride = stride;
+    if ((rc = rg::launch_sweep_large(a, s, grid))) return rc;
+  } else if ((rc = rg::launch_sweep(a, s, w->sm_count))) {
+    return rc;
+  }
   int32_t st = 0;
   RG_CUDA(cudaMemcpyAsync(&st, d_status, sizeof st, cudaMemcpyDeviceToHost, s));
   if (h_teig) RG_CUDA(cudaMemcpyAsync(h_teig, d_teig, sizeof(double) * w->neigv, cudaMemcpyDeviceToHost, s));
@@ -746,6 +805,15 @@ int rg_tdistrib_batch(rg_waveguide* w, const int32_t* seeds, int n, double* tall
   if (status) std::memcpy(status, st_host.data(), sizeof(int32_t) * n);
   const int bad = first_bad_status(st_host.data(), n);
   if (bad) return rg::fail(bad, status_text(bad));
+  return RG_OK;
+}
+
+int rg_last_sweep_time(rg_waveguide* w, float* ms) {
+  if (!w || !ms) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_sweep_time: NULL argument");
+  if (!w->sweep_timed) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_sweep_time: no single-launch batch timed yet");
+  DeviceGuard g(w->device);
+  RG_CUDA(cudaEventSynchronize(w->ev_sweep1));
+  RG_CUDA(cudaEventElapsedTime(ms, w->ev_sweep0, w->ev_sweep1));
   return RG_OK;
 }
 

@@ -150,3 +150,63 @@ def test_errors_are_statuses_not_crashes():
     assert e.value.code == rg.RG_ERR_SINGULAR
     T = g.tdistrib_upot(g.potential(1))
     assert np.all(np.isfinite(T))
+
+
+# Many-mode guides go through the blocked large-mode kernel (matrices in
+# global memory, potential drawn in-kernel on the seed path).  Short guides
+# keep the oracle fast; the slice matrices have the configs' full sizes:
+# M=128/ny=512 (differentiation config), M=256/ny=1024 (largest uneven
+# width) and M=512/ny=2048 (large sweep config).
+LARGE = {
+    "m72": dict(boundtype="dirichlet", nxdiso=40, nxfree=2, wol=36.25, exfac=1.0, aratio=1.0, dscat=6.0, ny=96),
+    "m81_periodic": dict(boundtype="periodic", nxdiso=30, nxfree=0, wol=40.3, exfac=1.0, aratio=1.0, dscat=4.0),
+    "m100_ragged_abs": dict(boundtype="dirichlet", nxdiso=25, nxfree=0, wol=50.25, exfac=1.0, aratio=1.0,
+                            dscat=8.0, dabso=1.0, napera=0.7, naperb=0.9, ny=200),
+    "m128": dict(boundtype="dirichlet", nxdiso=30, nxfree=0, wol=64.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=512),
+    "m256": dict(boundtype="dirichlet", nxdiso=8, nxfree=0, wol=128.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=1024),
+    "m512": dict(boundtype="dirichlet", nxdiso=4, nxfree=0, wol=256.25, exfac=1.0, aratio=1.0, dscat=20.0, ny=2048),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(LARGE))
+def large_pair(request):
+    kw = LARGE[request.param]
+    return request.param, O.Waveguide(**kw), rg.Waveguide(**kw)
+
+
+def test_large_tdistrib_upot_parity(large_pair):
+    name, o, g = large_pair
+    u = o.potential(5)
+    To, to = o.tdistrib_upot(u, want_t=True)
+    Tg, tg = g.tdistrib_upot(u, want_t=True)
+    assert relerr(tg, to) <= T_REL, name
+    assert np.max(np.abs(Tg - To)) <= TN_ABS, name
+
+
+def test_large_seed_path(large_pair):
+    """The in-kernel draw must reproduce the oracle's potential stream."""
+    name, o, g = large_pair
+    tall = np.zeros(2 * g.neigv)
+    g.compute_tdistrib(2, tall)
+    ref = o.tdistrib_upot(o.potential(2))
+    assert np.all(tall[: g.neigv] == 0)
+    assert np.max(np.abs(tall[g.neigv:] - ref)) <= TN_ABS, name
+
+
+def test_large_refl_trans_v1_t():
+    kw = LARGE["m72"]
+    o, g = O.Waveguide(**kw), rg.Waveguide(**kw)
+    u = o.potential(9)
+    _, to = o.refl_trans_v1_upot(u)
+    assert relerr(g.refl_trans_v1_upot(u), to) <= T_REL
+
+
+def test_large_batch_matches_single():
+    kw = dict(LARGE["m72"], nxdiso=12)
+    g = rg.Waveguide(**kw)
+    seeds = np.array([4, 2, 11], np.int32)
+    b = g.tdistrib_batch(seeds)
+    for k, s in enumerate(seeds):
+        one = np.zeros(s * g.neigv)
+        g.compute_tdistrib(int(s), one)
+        np.testing.assert_array_equal(b[k * g.neigv:(k + 1) * g.neigv], one[(s - 1) * g.neigv:])
