@@ -127,6 +127,18 @@ int rg_tdistrib_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* tal
 int rg_tdistrib_batch_device(rg_waveguide* wg, const int32_t* d_seeds, int n, double* d_tallvals,
                              int32_t* d_status, void* stream);
 
+/* Batched tdistrib over several waveguides at once (realizations of guides
+ * of uneven size; the reference would run one OpenMP seed loop per guide,
+ * src/main.f90:134-179): item k is realization seeds[k] of waveguide wgs[k],
+ * and its neigv eigenvalues (descending) go to tallvals[offsets[k] ...],
+ * which must lie inside tallvals[len].  Host arrays.  Items are grouped by
+ * kernel class (up to 16, 32, 64 modes, more), ordered by decreasing cost
+ * within a group, and each group runs as one persistent launch on wgs[0]'s
+ * stream; all handles must share a device.  status[k] (may be NULL) gets the
+ * per-item status; the first non-OK status is returned after all items ran. */
+int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, const int64_t* offsets,
+                      double* tallvals, int64_t len, int32_t* status);
+
 /* Tracing (the reference times its seed loop with date_and_time,
  * src/main.f90:145,174-176): device time in milliseconds of the sweep kernel
  * launched by the last rg_tdistrib_batch[_device] call on this handle,
@@ -143,8 +155,9 @@ int rg_last_sweep_time(rg_waveguide* wg, float* ms);
  * buffers d_teigvals[neigv] and d_status[1]; work is enqueued on `stream`
  * (NULL: the handle's stream) and the call returns without synchronising.
  * The potential is drawn into a fixed 16 MiB device array of the library,
- * shared by all calls, so nxdiso*ny may be at most 2,097,120; larger guides
- * get RG_ERR_INVALID_ARG.  The handle's device must be current; the first
+ * shared by all calls, so nxdiso*ny may be at most 2,097,120 (above 64 modes
+ * the elimination matrices, about 64*nmu^2 bytes, share the array too);
+ * larger guides get RG_ERR_INVALID_ARG.  The handle's device must be current; the first
  * call on each device looks the array up (make it before any stream capture).
  * Calls that overlap on the GPU race on the shared array. */
 int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_teigvals, int32_t* d_status, void* stream);

@@ -26,7 +26,7 @@ EXPORTS = (
     "rg_get_ny", "rg_get_nprop", "rg_get_window", "rg_get_xmesh", "rg_get_parameters", "rg_get_scalars",
     "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
-    "rg_tdistrib_seed_noalloc", "rg_last_sweep_time",
+    "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi",
 )
 
 
@@ -74,6 +74,7 @@ def lib() -> C.CDLL:
     L.rg_histogram.argtypes = [dp, i64, dp, C.c_int, dp, dp]
     L.rg_tdistrib_seed_noalloc.argtypes = [vp, C.c_int, vp, vp, vp]
     L.rg_last_sweep_time.argtypes = [vp, C.POINTER(C.c_float)]
+    L.rg_tdistrib_multi.argtypes = [C.POINTER(vp), ip, C.c_int, C.POINTER(C.c_int64), dp, i64, ip]
     _LIB = L
     return L
 
@@ -208,6 +209,32 @@ class Waveguide:
             return out, st
         _check(rc)
         return out
+
+
+def tdistrib_multi(items, return_status: bool = False):
+    """Eigenvalues of many (waveguide, seed) items in grouped persistent
+    launches.  items: sequence of (Waveguide, seed).  Returns a list of
+    per-item eigenvalue arrays (and the status array if asked)."""
+    n = len(items)
+    if n == 0:
+        return ([], np.zeros(0, np.int32)) if return_status else []
+    offs = np.zeros(n, np.int64)
+    tot = 0
+    for k, (w, _) in enumerate(items):
+        offs[k] = tot
+        tot += w.neigv
+    handles = (C.c_void_p * n)(*[w._h for w, _ in items])
+    seeds = np.ascontiguousarray([s for _, s in items], np.int32)
+    out = np.zeros(tot, np.float64)
+    st = np.zeros(n, np.int32)
+    ip = C.POINTER(C.c_int32)
+    rc = lib().rg_tdistrib_multi(handles, seeds.ctypes.data_as(ip), n, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                 _dp(out), tot, st.ctypes.data_as(ip))
+    res = [out[offs[k]: offs[k] + w.neigv].copy() for k, (w, _) in enumerate(items)]
+    if return_status:
+        return res, st
+    _check(rc)
+    return res
 
 
 def histogram(samples, bins):

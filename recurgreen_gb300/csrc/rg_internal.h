@@ -29,36 +29,46 @@ int cuda_fail(cudaError_t e, const char* what);
 // Largest mode count the shared-memory sweep kernel handles.
 constexpr int kMaxModesSmem = 64;
 
-// Everything one launch of the sweep kernel needs.  Device pointers.
-struct SweepArgs {
+// One waveguide as the kernels see it: sizes and device tables, built by
+// rg_init and kept in device memory for the handle's lifetime.
+struct WgDesc {
   int M;        // nmu
   int ny;       // transverse grid points
   int nx;       // total slices
   int nxdiso;   // disordered slices
   int nxfree;   // free slices on each side
-  int row0, nrow, col0, ncol;  // Fisher-Lee window, 0-based start and extent
+  int row0, nrow, col0, ncol;  // tdistrib Fisher-Lee window, 0-based start and extent
   int neigv;    // eigenvalues kept per realization
-  int mode;     // kModeEig or kModeTmat
-  int nreal;    // realizations in this launch
+  int periodic;
+  double stdu;                // standard deviation of the dimensionless potential
   const double2* bmat;        // [M] B diagonal
   const double2* adiag_edge;  // [M] A diagonal on slices 1 and nx
   const double2* adiag_bulk;  // [M] A diagonal in the bulk
-  const double2* sqmu;        // [M] Fisher-Lee weights
-  const double* costab;       // [(2M+1) * ny] cos(pi d y_j) / ny  (Dirichlet)
-  const double2* expfac;      // [M * ny] exp(2 pi i d y_j) / ny  (periodic), d = 0..M-1
-  int periodic;
-  const double* upot;         // potential, element (r, ix, iy) at r*pot_rstride + ix*pot_xstride + iy*pot_ystride
+  const double2* sqmu_c;      // [M] complex sqrt(mu) (tdistrib Fisher-Lee)
+  const double2* sqmu_r;      // [M] sqrt(real(mu)) (v1 Fisher-Lee)
+  const double* costab;       // [ny * (2M+1)] cos(pi d y_j) / ny  (Dirichlet)
+  const double2* expfac;      // [ny * M] exp(2 pi i d y_j) / ny  (periodic), d = 0..M-1
+  const uint64_t* jumppoly;   // [ny * 4] x^(2*nxdiso*iy) mod the xoshiro256 characteristic polynomial
+};
+
+// One launch of a sweep kernel: a queue of work items (realizations), each a
+// (waveguide, seed) pair.  Device pointers.
+struct SweepArgs {
+  int mode;                   // kModeEig or kModeTmat
+  int nreal;                  // work items in this launch
+  const WgDesc* wgs;          // waveguides
+  const int32_t* item_wg;     // [nreal] waveguide of each item; nullptr: all use wgs[0]
+  const int32_t* seeds;       // [nreal] seeds; the potential is drawn in-kernel when upot == nullptr
+  const double* upot;         // optional potentials, (r, ix, iy) at r*pot_rstride + ix*pot_xstride + iy*pot_ystride
   int64_t pot_rstride, pot_xstride, pot_ystride;
-  double* teig;               // [nreal * neigv] (kModeEig)
-  double2* tout;              // [nreal * nrow * ncol] column-major t (optional)
+  const int64_t* teig_off;    // [nreal] offset of item r's eigenvalues in teig; nullptr: r * neigv
+  double* teig;               // eigenvalues (kModeEig)
+  double2* tout;              // [nreal][nrow * ncol] column-major t, optional (items of one waveguide only)
   int32_t* status;            // [nreal]
   int* work_counter;          // persistent-scheduling counter, zeroed before launch
-  // Large-mode kernel (M > kMaxModesSmem) only:
-  const int32_t* seeds;       // [nreal] seeds; the potential is drawn in-kernel when upot == nullptr
-  const uint64_t* jumppoly;   // [ny * 4] jump polynomials for the in-kernel draw
-  double stdu;                // potential standard deviation for the in-kernel draw
   double2* work;              // per-CTA workspace in global memory
   int64_t work_stride;        // double2 elements per CTA
+  int max_M, max_ny;          // largest M and ny among the items (shared-memory sizing)
 };
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
@@ -73,10 +83,13 @@ struct PotArgs {
   double* upot;                // [nreal][nxdiso][ny]
 };
 
-// Launchers (rg_sweep.cu).  All enqueue on `stream`.
+// Launchers.  All enqueue on `stream`.  A sweep launch is planned first (grid
+// size and per-CTA workspace, from max_M/max_ny and the kernel's occupancy),
+// then launched with a.work pointing at grid * work_stride double2 elements.
 int launch_potential(const PotArgs& a, cudaStream_t stream);
-int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count);
-// Large-mode sweep (rg_sweep_large.cu): grid size and workspace it needs, and the launch.
+int sweep_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid);
+// The large-mode kernel behind sweep_plan/launch_sweep for max_M > kMaxModesSmem (rg_sweep_large.cu).
 int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
@@ -86,13 +99,13 @@ int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, i
 void jump_polynomial(uint64_t distance, uint64_t out[4]);
 
 // Read-only view of a handle for the allocation-free entry point
-// (rg_noalloc.cu): sizes, device tables and the base sweep arguments.
+// (rg_noalloc.cu): sizes, device tables and the device-resident descriptor.
 struct NoAllocView {
-  int device, sm_count, nxdiso, ny;
+  int device, sm_count, nxdiso, ny, nmu;
   double stdu;
   const uint64_t* jumppoly;
   cudaStream_t stream;
-  SweepArgs sweep;
+  const WgDesc* d_desc;
 };
 int noalloc_view(const rg_waveguide* w, NoAllocView* out);
 

@@ -10,9 +10,10 @@
 // then call this entry point, which only launches kernels on memory that
 // already exists.
 //
-// The per-call scratch (the disorder potential of the realization, the seed
-// and the work-queue counter) lives in a file-scope __device__ array of fixed
-// size, kNoAllocScratchBytes = 16 MiB.  Every GPU that loads this library
+// The per-call scratch (the disorder potential of the realization, the seed,
+// the work-queue counter and, above 64 modes, the elimination matrices) lives
+// in a file-scope __device__ array of fixed size, kNoAllocScratchBytes =
+// 16 MiB.  Every GPU that loads this library
 // holds that array until the process exits.  Its device address is looked up
 // with cudaGetSymbolAddress once per device, on the first call made with that
 // device current; make that first call before any stream capture begins.
@@ -28,7 +29,6 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
 constexpr size_t kNoAllocHeaderBytes = 256;         // seed, counter
-constexpr size_t kNoAllocPotentialDoubles = (kNoAllocScratchBytes - kNoAllocHeaderBytes) / sizeof(double);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -67,12 +67,28 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   rg::NoAllocView v{};
   int rc = rg::noalloc_view(wg, &v);
   if (rc) return rc;
-  const size_t need = (size_t)v.nxdiso * (size_t)v.ny;
-  if (need > kNoAllocPotentialDoubles)
+  // The sweep's launch arguments: one item, the potential read from the array.
+  rg::SweepArgs a{};
+  a.mode = rg::kModeEig;
+  a.nreal = 1;
+  a.wgs = v.d_desc;
+  a.max_M = v.nmu;
+  a.max_ny = v.ny;
+  a.teig = d_teigvals;
+  a.status = d_status;
+  int grid = 1;
+  int64_t stride = 0;
+  if ((rc = rg::sweep_plan(a, v.sm_count, &grid, &stride))) return rc;
+  // Above 64 modes the elimination also needs its matrices in the array.
+  const bool large = v.nmu > rg::kMaxModesSmem;
+  const size_t pot_doubles = (size_t)v.nxdiso * (size_t)v.ny;
+  const size_t pot_bytes = (pot_doubles * sizeof(double) + 255) & ~(size_t)255;
+  const size_t ws_bytes = large ? sizeof(double2) * (size_t)stride * grid : 0;
+  if (pot_bytes + ws_bytes > kNoAllocScratchBytes - kNoAllocHeaderBytes)
     return rg::fail(RG_ERR_INVALID_ARG,
-                    "rg_tdistrib_seed_noalloc: nxdiso*ny = " + std::to_string(need) +
-                        " exceeds the fixed scratch capacity of " + std::to_string(kNoAllocPotentialDoubles) +
-                        " doubles (16 MiB); use rg_compute_tdistrib");
+                    "rg_tdistrib_seed_noalloc: nxdiso*ny = " + std::to_string(pot_doubles) +
+                        " potential doubles" + (large ? " plus the elimination workspace" : "") +
+                        " exceed the fixed scratch capacity of 16 MiB; use rg_compute_tdistrib");
   int cur = -1;
   cudaError_t e = cudaGetDevice(&cur);
   if (e != cudaSuccess) return rg::cuda_fail(e, "cudaGetDevice");
@@ -97,15 +113,12 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   pa.jumppoly = v.jumppoly;
   pa.upot = d_pot;
   if ((rc = rg::launch_potential(pa, s))) return rc;
-  rg::SweepArgs a = v.sweep;
-  a.nreal = 1;
   a.upot = d_pot;
   a.pot_rstride = 0;
   a.pot_xstride = v.ny;
   a.pot_ystride = 1;
-  a.teig = d_teigvals;
-  a.tout = nullptr;
-  a.status = d_status;
   a.work_counter = d_counter;
-  return rg::launch_sweep(a, s, v.sm_count);
+  a.work = large ? reinterpret_cast<double2*>(base + kNoAllocHeaderBytes + pot_bytes) : nullptr;
+  a.work_stride = large ? stride : 0;
+  return rg::launch_sweep(a, s, grid);
 }

@@ -43,11 +43,12 @@ __global__ void potential_kernel(PotArgs a) {
 // Sweep kernel
 // ---------------------------------------------------------------------------
 //
-// One realization per CTA; persistent CTAs take realizations from a work
-// counter.  Per slice the kernel solves X Y = R for the slice matrix
-// X = A_n - V_n - B Gss B and the right-hand side R = B Gs1 by Gauss-Jordan
-// elimination, which leaves inv(X) = Gss in W and Y in R, so the new
-// propagator is Gs1 = -Y.
+// One work item (a realization of one waveguide) per CTA; persistent CTAs
+// take items from a work counter, so one launch can mix waveguides of
+// different sizes up to MCAP modes.  Per slice the kernel solves X Y = R for
+// the slice matrix X = A_n - V_n - B Gss B and the right-hand side
+// R = B Gs1 by Gauss-Jordan elimination, which leaves inv(X) = Gss in W and
+// Y in R, so the new propagator is Gs1 = -Y.
 //
 // W (M x M complex) lives in shared memory (row stride LDW = MCAP + 1);
 // R (M x M complex) lives in registers: thread (warp w, lane l) owns
@@ -64,20 +65,27 @@ __global__ void potential_kernel(PotArgs a) {
 // next slice keeps every R row in place: physical row q then carries logical
 // row pinv[q], so R is only rescaled by B, and W is rebuilt by a gather that
 // stays inside each row.
-template <int MCAP, int NT>
+//
+// The disorder is drawn in the kernel: each transverse column iy has its own
+// xoshiro256** state (jumped to the column's start in the reference stream)
+// in the CTA's workspace, advanced by two draws per disordered slice.
+template <int MCAP>
 struct SweepSmem {
   static constexpr int LDW = MCAP + 1;
-  static size_t bytes(int ny) {
-    const int nyp = (ny + 1) & ~1;
+  static size_t bytes(int max_ny) {
+    const int nyp = (max_ny + 1) & ~1;
     return sizeof(double2) * ((size_t)MCAP * LDW + 3 * MCAP) + sizeof(double) * (2 * MCAP + 2 + nyp) +
            sizeof(int) * 5 * MCAP;
   }
 };
 
+// Per-CTA workspace of the shared-memory kernel: generator states only.
+inline int64_t small_stride(int max_ny) { return ((2 * (int64_t)max_ny) + 15) & ~(int64_t)15; }
+
 template <int MCAP, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
   constexpr int NW = NT / 32;
-  constexpr int LDW = SweepSmem<MCAP, NT>::LDW;
+  constexpr int LDW = SweepSmem<MCAP>::LDW;
   constexpr int AMAX = (MCAP + NW - 1) / NW;  // rows per warp
   constexpr int CB = (MCAP + 31) / 32;        // column blocks per lane
   constexpr int TMAX = (MCAP * MCAP + NT - 1) / NT;
@@ -87,24 +95,31 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
   double2* rowW = colbuf + MCAP;               // [MCAP] scaled pivot row of W
   double2* rowR = rowW + MCAP;                 // [MCAP] scaled pivot row of R
   double* cc = (double*)(rowR + MCAP);         // [2*MCAP+2] projection coefficients
-  double* urow = cc + (2 * MCAP + 2);          // [ny] potential of the slice
-  int* piv = (int*)(urow + ((a.ny + 1) & ~1)); // [MCAP] pivot row of column k
+  double* urow = cc + (2 * MCAP + 2);          // [max_ny] potential of the slice
+  int* piv = (int*)(urow + ((a.max_ny + 1) & ~1));  // [MCAP] pivot row of column k
   int* pinv = piv + MCAP;                      // [MCAP] column of which row q was pivot
   int* sinv = pinv + MCAP;                     // [MCAP] physical row of logical row c
   int* colmap = sinv + MCAP;                   // [MCAP] W column holding Gss column c
   int* used = colmap + MCAP;                   // [MCAP]
   __shared__ int s_r, s_p, s_status, s_rot;
   __shared__ double2 s_d;
+  __shared__ WgDesc wd;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int M = a.M;
+  uint64_t* gen = (uint64_t*)(a.work + (int64_t)blockIdx.x * a.work_stride);  // [max_ny][4]
+  const bool draw = (a.upot == nullptr);
+  const bool tmat = (a.mode == kModeTmat);
   double2 R[AMAX][CB];
 
   for (;;) {
-    if (tid == 0) s_r = atomicAdd(a.work_counter, 1);
+    if (tid == 0) {
+      s_r = atomicAdd(a.work_counter, 1);
+      if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
+    }
     __syncthreads();
     const int r = s_r;
     if (r >= a.nreal) break;
+    const int M = wd.M, ny = wd.ny, nx = wd.nx;
     if (tid == 0) s_status = RG_OK;
     for (int c = tid; c < M; c += NT) {
       sinv[c] = c;
@@ -115,40 +130,60 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
 #pragma unroll
       for (int b = 0; b < CB; ++b)
         R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? 1.0 : 0.0, 0.0);
-    const double* U = a.upot + (int64_t)r * a.pot_rstride;
+    if (draw) {
+      for (int iy = tid; iy < ny; iy += NT) {
+        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
+        gen[4 * iy + 0] = st.s0;
+        gen[4 * iy + 1] = st.s1;
+        gen[4 * iy + 2] = st.s2;
+        gen[4 * iy + 3] = st.s3;
+      }
+    }
+    const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;
     __syncthreads();
 
-    for (int n = 0; n < a.nx; ++n) {
-      const int id = n - a.nxfree;
-      const bool dis = (id >= 0 && id < a.nxdiso);
+    for (int n = 0; n < nx; ++n) {
+      const int id = n - wd.nxfree;
+      const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
-        // 1. Projection coefficients of this slice's potential.
-        for (int j = tid; j < a.ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+        // 1. This slice's potential row (drawn or loaded) and its projection.
+        if (draw) {
+          for (int iy = tid; iy < ny; iy += NT) {
+            Xoshiro st{gen[4 * iy], gen[4 * iy + 1], gen[4 * iy + 2], gen[4 * iy + 3]};
+            urow[iy] = scaled_normal(wd.stdu, st);
+            gen[4 * iy + 0] = st.s0;
+            gen[4 * iy + 1] = st.s1;
+            gen[4 * iy + 2] = st.s2;
+            gen[4 * iy + 3] = st.s3;
+          }
+        } else {
+          for (int j = tid; j < ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+        }
         __syncthreads();
-        if (!a.periodic) {
+        if (!wd.periodic) {
           // cc[d] = (1/ny) sum_j U_j cos(pi d y_j), d = 0..2M, so that
           // (modal^T diag(U) modal)[a][c] = cc[|a-c|] - cc[a+c+2].
           const int nd = 2 * M + 1;
           for (int d = tid; d < nd; d += NT) {
-            const double* ct = a.costab + d;
+            const double* ct = wd.costab + d;
             double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
             int j = 0;
-            for (; j + 4 <= a.ny; j += 4) {
+            for (; j + 4 <= ny; j += 4) {
               s0 = fma(ct[(int64_t)(j + 0) * nd], urow[j + 0], s0);
               s1 = fma(ct[(int64_t)(j + 1) * nd], urow[j + 1], s1);
               s2 = fma(ct[(int64_t)(j + 2) * nd], urow[j + 2], s2);
               s3 = fma(ct[(int64_t)(j + 3) * nd], urow[j + 3], s3);
             }
-            for (; j < a.ny; ++j) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
+            for (; j < ny; ++j) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
             cc[d] = (s0 + s1) + (s2 + s3);
           }
         } else {
           // f[d] = (1/ny) sum_j U_j exp(2 pi i d y_j), d = 0..M-1, so that
           // (modal^H diag(U) modal)[a][c] = f[c-a] (c >= a), conj(f[a-c]) else.
           for (int d = tid; d < M; d += NT) {
-            const double2* et = a.expfac + d;
+            const double2* et = wd.expfac + d;
             double sr = 0.0, si = 0.0;
-            for (int j = 0; j < a.ny; ++j) {
+            for (int j = 0; j < ny; ++j) {
               const double2 e = et[(int64_t)j * M];
               sr = fma(e.x, urow[j], sr);
               si = fma(e.y, urow[j], si);
@@ -162,14 +197,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
 
       // 2. Assemble X = A_n - V_n - B Gss B in physical row order (W), and
       //    R = B Gs1 (identity on the first slice; registers, in place).
-      const double2* adiag = (n == 0 || n == a.nx - 1) ? a.adiag_edge : a.adiag_bulk;
+      const double2* adiag = (n == 0 || n == nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
       const double rsign = (n == 1) ? 1.0 : -1.0;  // Gs1 = +Y after slice 1, -Y after later slices
 #pragma unroll
       for (int ai = 0; ai < AMAX; ++ai) {
         const int q = warp + NW * ai;
         if (q < M) {
           const int al = (n == 0) ? q : pinv[q];  // logical row carried by physical row q
-          const double2 ba = a.bmat[al];
+          const double2 ba = wd.bmat[al];
           double2 v[CB];
 #pragma unroll
           for (int b = 0; b < CB; ++b) {
@@ -179,7 +214,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
               if (al == c) x = adiag[c];
               if (dis) {
                 double2 vac;
-                if (!a.periodic) {
+                if (!wd.periodic) {
                   const int dd = al > c ? al - c : c - al;
                   vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
                 } else {
@@ -188,7 +223,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
                 }
                 x = csub(x, vac);
               }
-              if (n > 0) x = csub(x, cmul(cmul(ba, W[q * LDW + colmap[c]]), a.bmat[c]));
+              if (n > 0) x = csub(x, cmul(cmul(ba, W[q * LDW + colmap[c]]), wd.bmat[c]));
               if (n > 0) R[ai][b] = cmul(ba, cscale(rsign, R[ai][b]));
             }
             v[b] = x;
@@ -318,8 +353,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
       }
     }
     __syncthreads();
-    const double gsign = (a.nx >= 2) ? -1.0 : 1.0;
-    const int nrow = a.nrow, ncol = a.ncol;
+    const double gsign = (nx >= 2) ? -1.0 : 1.0;
+    const int row0 = tmat ? 0 : wd.row0, col0 = tmat ? 0 : wd.col0;
+    const int nrow = tmat ? M : wd.nrow, ncol = tmat ? M : wd.ncol;
+    const double2* sqmu = tmat ? wd.sqmu_r : wd.sqmu_c;
     double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
     double2 tv[TMAX];
 #pragma unroll
@@ -328,16 +365,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
       tv[s] = make_double2(0.0, 0.0);
       if (e < nrow * ncol) {
         const int i = e % nrow, j = e / nrow;
-        const int gi = a.row0 + i, gj = a.col0 + j;
+        const int gi = row0 + i, gj = col0 + j;
         const double2 g = cscale(gsign, W[piv[gi] * LDW + gj]);
-        const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
+        const double2 v = cmul(cmul(sqmu[gi], g), sqmu[gj]);
         tv[s] = make_double2(-2.0 * v.y, 2.0 * v.x);  // (0, 2) * v
         if (tout) tout[e] = tv[s];
       }
     }
     __syncthreads();
 
-    if (a.mode == kModeEig) {
+    if (!tmat) {
 #pragma unroll
       for (int s = 0; s < TMAX; ++s) {
         const int e = tid + NT * s;
@@ -416,6 +453,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
         if (lane == 0) cc[k] = s;
       }
       __syncthreads();
+      const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
       for (int k = tid; k < nv; k += NT) {
         const double tk = cc[k];
         int rank = 0;
@@ -423,7 +461,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
           const double tj = cc[j];
           rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
         }
-        if (rank < a.neigv) a.teig[(int64_t)r * a.neigv + rank] = tk;
+        if (rank < wd.neigv) a.teig[obase + rank] = tk;
       }
     }
     __syncthreads();
@@ -462,15 +500,22 @@ __global__ void histogram_kernel(const double* __restrict__ x, int64_t n, const 
 }
 
 template <int MCAP, int NT, int MINB>
-int launch_sweep_t(const SweepArgs& a, cudaStream_t stream, int sm_count) {
-  const size_t smem = SweepSmem<MCAP, NT>::bytes(a.ny);
+int plan_t(const SweepArgs& a, int sm_count, int* grid, int64_t* stride) {
+  const size_t smem = SweepSmem<MCAP>::bytes(a.max_ny);
   RG_CUDA(cudaFuncSetAttribute(sweep_kernel<MCAP, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<MCAP, NT, MINB>, NT, smem));
   if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "sweep kernel does not fit on an SM (ny too large?)");
-  int grid = per_sm * sm_count;
-  if (grid > a.nreal) grid = a.nreal;
-  sweep_kernel<MCAP, NT, MINB><<<grid, NT, smem, stream>>>(a);
+  int g = per_sm * sm_count;
+  if (g > a.nreal) g = a.nreal;
+  *grid = g < 1 ? 1 : g;
+  *stride = small_stride(a.max_ny);
+  return RG_OK;
+}
+
+template <int MCAP, int NT, int MINB>
+int launch_t(const SweepArgs& a, cudaStream_t stream, int grid) {
+  sweep_kernel<MCAP, NT, MINB><<<grid, NT, SweepSmem<MCAP>::bytes(a.max_ny), stream>>>(a);
   RG_CUDA(cudaGetLastError());
   return RG_OK;
 }
@@ -485,12 +530,19 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
   return RG_OK;
 }
 
-int launch_sweep(const SweepArgs& a, cudaStream_t stream, int sm_count) {
+int sweep_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+  if (a.max_M <= 16) return plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
+  if (a.max_M <= 32) return plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
+  if (a.max_M <= kMaxModesSmem) return plan_t<64, 256, 2>(a, sm_count, grid, work_stride);
+  return sweep_large_plan(a, sm_count, grid, work_stride);
+}
+
+int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  if (a.M <= 16) return launch_sweep_t<16, 64, 8>(a, stream, sm_count);
-  if (a.M <= 32) return launch_sweep_t<32, 128, 4>(a, stream, sm_count);
-  if (a.M <= kMaxModesSmem) return launch_sweep_t<64, 256, 2>(a, stream, sm_count);
-  return fail(RG_ERR_INVALID_ARG, "nmu > 64 goes through the large-mode kernel");
+  if (a.max_M <= 16) return launch_t<16, 64, 8>(a, stream, grid);
+  if (a.max_M <= 32) return launch_t<32, 128, 4>(a, stream, grid);
+  if (a.max_M <= kMaxModesSmem) return launch_t<64, 256, 2>(a, stream, grid);
+  return launch_sweep_large(a, stream, grid);
 }
 
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,

@@ -43,40 +43,46 @@ inline int64_t large_stride(int M, int ny) {
 
 __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
   constexpr int NT = kLargeNT, NB = kLargeNB, NW = NT / 32;
-  const int M = a.M, ny = a.ny;
-  const int64_t mm = (int64_t)M * M;
+  const int MX = a.max_M;
   extern __shared__ double2 sm[];
   double2* P = sm;                          // [M][NB] current panel
-  double2* Ub = P + M * NB;                 // [M][NB] multipliers of the panel's steps
-  double2* Lt = Ub + M * NB;                // [NB][NB] Lt[k][l] = u_l[p_k], l < k
+  double2* Ub = P + MX * NB;                // [M][NB] multipliers of the panel's steps
+  double2* Lt = Ub + MX * NB;               // [NB][NB] Lt[k][l] = u_l[p_k], l < k
   double2* colf = Lt + NB * NB;             // [M] panel column before the step
-  double2* rowp = colf + M;                 // [NB] scaled pivot row inside the panel
+  double2* rowp = colf + MX;                // [NB] scaled pivot row inside the panel
   double* cc = (double*)(rowp + NB);        // [2M+2] projection coefficients
-  double* urow = cc + (2 * M + 2);          // [ny] potential of the slice
-  int* piv = (int*)(urow + ((ny + 1) & ~1));
-  int* pinv = piv + M;
-  int* sinv = pinv + M;
-  int* colmap = sinv + M;
-  int* used = colmap + M;
+  double* urow = cc + (2 * MX + 2);         // [ny] potential of the slice
+  int* piv = (int*)(urow + ((a.max_ny + 1) & ~1));
+  int* pinv = piv + MX;
+  int* sinv = pinv + MX;
+  int* colmap = sinv + MX;
+  int* used = colmap + MX;
   __shared__ int s_r, s_p, s_status, s_rot;
   __shared__ double2 s_d;
   __shared__ unsigned long long s_key[NW];
   __shared__ int s_idx[NW];
+  __shared__ WgDesc wd;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  double2* ws = a.work + (int64_t)blockIdx.x * a.work_stride;
-  double2* const Wb0 = ws;
-  double2* const Wb1 = ws + mm;
-  double2* Rg = ws + 2 * mm;
-  double2* Tg = ws + 3 * mm;
-  uint64_t* gen = (uint64_t*)(ws + 4 * mm);  // [ny][4]
   const bool draw = (a.upot == nullptr);
+  const bool tmat = (a.mode == kModeTmat);
 
   for (;;) {
-    if (tid == 0) s_r = atomicAdd(a.work_counter, 1);
+    if (tid == 0) {
+      s_r = atomicAdd(a.work_counter, 1);
+      if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
+    }
     __syncthreads();
     const int r = s_r;
     if (r >= a.nreal) break;
+    const int M = wd.M, ny = wd.ny;
+    const int64_t mm = (int64_t)M * M;
+    double2* ws = a.work + (int64_t)blockIdx.x * a.work_stride;
+    double2* const Wb0 = ws;
+    double2* const Wb1 = ws + mm;
+    double2* Rg = ws + 2 * mm;
+    double2* Tg = ws + 3 * mm;
+    uint64_t* gen = (uint64_t*)(ws + 4 * mm);  // [ny][4]
     if (tid == 0) s_status = RG_OK;
     for (int c = tid; c < M; c += NT) {
       sinv[c] = c;
@@ -85,7 +91,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
     for (int64_t e = tid; e < mm; e += NT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
     if (draw) {
       for (int iy = tid; iy < ny; iy += NT) {
-        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), a.jumppoly + 4 * (int64_t)iy);
+        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
         gen[4 * iy + 0] = st.s0;
         gen[4 * iy + 1] = st.s1;
         gen[4 * iy + 2] = st.s2;
@@ -96,15 +102,15 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
     __syncthreads();
 
     int cur = 0;
-    for (int n = 0; n < a.nx; ++n) {
-      const int id = n - a.nxfree;
-      const bool dis = (id >= 0 && id < a.nxdiso);
+    for (int n = 0; n < wd.nx; ++n) {
+      const int id = n - wd.nxfree;
+      const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
         // 1. This slice's potential row (drawn or loaded) and its projection.
         if (draw) {
           for (int iy = tid; iy < ny; iy += NT) {
             Xoshiro st{gen[4 * iy], gen[4 * iy + 1], gen[4 * iy + 2], gen[4 * iy + 3]};
-            urow[iy] = scaled_normal(a.stdu, st);
+            urow[iy] = scaled_normal(wd.stdu, st);
             gen[4 * iy + 0] = st.s0;
             gen[4 * iy + 1] = st.s1;
             gen[4 * iy + 2] = st.s2;
@@ -114,10 +120,10 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           for (int j = tid; j < ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
         }
         __syncthreads();
-        if (!a.periodic) {
+        if (!wd.periodic) {
           const int nd = 2 * M + 1;
           for (int d = tid; d < nd; d += NT) {
-            const double* ct = a.costab + d;
+            const double* ct = wd.costab + d;
             double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
             int j = 0;
             for (; j + 4 <= ny; j += 4) {
@@ -131,7 +137,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           }
         } else {
           for (int d = tid; d < M; d += NT) {
-            const double2* et = a.expfac + d;
+            const double2* et = wd.expfac + d;
             double sr = 0.0, si = 0.0;
             for (int j = 0; j < ny; ++j) {
               const double2 e = et[(int64_t)j * M];
@@ -150,7 +156,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       double2* Wold = cur ? Wb1 : Wb0;
       double2* W = cur ? Wb0 : Wb1;
       cur ^= 1;
-      const double2* adiag = (n == 0 || n == a.nx - 1) ? a.adiag_edge : a.adiag_bulk;
+      const double2* adiag = (n == 0 || n == wd.nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
       const double rsign = (n == 1) ? 1.0 : -1.0;
       for (int64_t e = tid; e < mm; e += NT) {
         const int q = (int)(e / M), c = (int)(e % M);
@@ -158,7 +164,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         double2 x = (al == c) ? adiag[c] : make_double2(0.0, 0.0);
         if (dis) {
           double2 vac;
-          if (!a.periodic) {
+          if (!wd.periodic) {
             const int dd = al > c ? al - c : c - al;
             vac = make_double2(cc[dd] - cc[al + c + 2], 0.0);
           } else {
@@ -168,8 +174,8 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           x = csub(x, vac);
         }
         if (n > 0) {
-          x = csub(x, cmul(cmul(a.bmat[al], Wold[(int64_t)q * M + colmap[c]]), a.bmat[c]));
-          Rg[e] = cmul(a.bmat[al], cscale(rsign, Rg[e]));
+          x = csub(x, cmul(cmul(wd.bmat[al], Wold[(int64_t)q * M + colmap[c]]), wd.bmat[c]));
+          Rg[e] = cmul(wd.bmat[al], cscale(rsign, Rg[e]));
         }
         W[e] = x;
       }
@@ -326,21 +332,23 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
 
     // 5. Fisher-Lee: t = 2i sqmu_a Gs1 sqmu_j with Gs1[a][j] = sign * R[piv[a]][j];
     //    t goes to the workspace, column-major (ld = nrow).
-    const double gsign = (a.nx >= 2) ? -1.0 : 1.0;
-    const int nrow = a.nrow, ncol = a.ncol;
+    const double gsign = (wd.nx >= 2) ? -1.0 : 1.0;
+    const int row0 = tmat ? 0 : wd.row0, col0 = tmat ? 0 : wd.col0;
+    const int nrow = tmat ? M : wd.nrow, ncol = tmat ? M : wd.ncol;
+    const double2* sqmu = tmat ? wd.sqmu_r : wd.sqmu_c;
     double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
     for (int e = tid; e < nrow * ncol; e += NT) {
       const int i = e % nrow, j = e / nrow;
-      const int gi = a.row0 + i, gj = a.col0 + j;
+      const int gi = row0 + i, gj = col0 + j;
       const double2 g = cscale(gsign, Rg[(int64_t)piv[gi] * M + gj]);
-      const double2 v = cmul(cmul(a.sqmu[gi], g), a.sqmu[gj]);
+      const double2 v = cmul(cmul(sqmu[gi], g), sqmu[gj]);
       const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);
       Tg[e] = t;
       if (tout) tout[e] = t;
     }
     __syncthreads();
 
-    if (a.mode == kModeEig) {
+    if (!tmat) {
       // 6. Eigenvalues of t^H t: one-sided Jacobi on the vectors of the
       //    smaller dimension (columns of t, or its rows), in the workspace.
       const bool bycol = nrow >= ncol;
@@ -411,6 +419,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         if (lane == 0) cc[k] = s;
       }
       __syncthreads();
+      const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
       for (int k = tid; k < nv; k += NT) {
         const double tk = cc[k];
         int rank = 0;
@@ -418,7 +427,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           const double tj = cc[j];
           rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
         }
-        if (rank < a.neigv) a.teig[(int64_t)r * a.neigv + rank] = tk;
+        if (rank < wd.neigv) a.teig[obase + rank] = tk;
       }
     }
     __syncthreads();
@@ -429,7 +438,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
 }  // namespace
 
 int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
-  const size_t smem = LargeSmem::bytes(a.M, a.ny);
+  const size_t smem = LargeSmem::bytes(a.max_M, a.max_ny);
   if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes or transverse points for the large-mode kernel");
   RG_CUDA(cudaFuncSetAttribute(sweep_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -439,13 +448,13 @@ int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_
   if (g > a.nreal) g = a.nreal;
   if (g < 1) g = 1;
   *grid = g;
-  *work_stride = large_stride(a.M, a.ny);
+  *work_stride = large_stride(a.max_M, a.max_ny);
   return RG_OK;
 }
 
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  const size_t smem = LargeSmem::bytes(a.M, a.ny);
+  const size_t smem = LargeSmem::bytes(a.max_M, a.max_ny);
   sweep_large_kernel<<<grid, kLargeNT, smem, stream>>>(a);
   RG_CUDA(cudaGetLastError());
   return RG_OK;

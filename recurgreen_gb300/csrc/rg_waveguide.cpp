@@ -187,6 +187,8 @@ struct rg_waveguide {
   double2* d_expfac = nullptr;
   uint64_t* d_jump = nullptr;
   int* d_counter = nullptr;
+  rg::WgDesc h_desc{};           // the kernels' view of this waveguide (device pointers)
+  rg::WgDesc* d_desc = nullptr;  // its device copy
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
   cudaEvent_t ev_sweep0 = nullptr, ev_sweep1 = nullptr;  // around the last batch's sweep launches
@@ -231,6 +233,7 @@ void free_device(rg_waveguide* w) {
   cudaFree(w->d_expfac);
   cudaFree(w->d_jump);
   cudaFree(w->d_counter);
+  cudaFree(w->d_desc);
   cudaFree(w->d_scratch);
   if (w->ev_sweep0) cudaEventDestroy(w->ev_sweep0);
   if (w->ev_sweep1) cudaEventDestroy(w->ev_sweep1);
@@ -242,6 +245,7 @@ void free_device(rg_waveguide* w) {
   w->d_expfac = nullptr;
   w->d_jump = nullptr;
   w->d_counter = nullptr;
+  w->d_desc = nullptr;
   w->d_scratch = nullptr;
   w->scratch_bytes = 0;
   w->stream = nullptr;
@@ -374,6 +378,29 @@ int upload_tables(rg_waveguide* w) {
   if ((rc = upload(&w->d_expfac, w->expfac.data(), sizeof(double2) * w->expfac.size()))) return rc;
   if ((rc = upload(&w->d_jump, w->jump.data(), sizeof(uint64_t) * w->jump.size()))) return rc;
   RG_CUDA(cudaMalloc((void**)&w->d_counter, sizeof(int)));
+  rg::WgDesc d{};
+  d.M = w->nmu;
+  d.ny = w->ny;
+  d.nx = w->nx;
+  d.nxdiso = w->p.nxdiso;
+  d.nxfree = w->p.nxfree;
+  d.row0 = w->imin - 1;
+  d.nrow = w->imax - w->imin + 1;
+  d.col0 = w->jmin - 1;
+  d.ncol = w->jmax - w->jmin + 1;
+  d.neigv = w->neigv;
+  d.periodic = w->p.boundtype == RG_BOUND_PERIODIC;
+  d.stdu = w->stdu;
+  d.bmat = w->d_bmat;
+  d.adiag_edge = w->d_aedge;
+  d.adiag_bulk = w->d_abulk;
+  d.sqmu_c = w->d_sqmu_c;
+  d.sqmu_r = w->d_sqmu_r;
+  d.costab = w->d_costab;
+  d.expfac = w->d_expfac;
+  d.jumppoly = w->d_jump;
+  w->h_desc = d;
+  if ((rc = upload(&w->d_desc, &d, sizeof d))) return rc;
   RG_CUDA(cudaEventCreate(&w->ev_sweep0));
   RG_CUDA(cudaEventCreate(&w->ev_sweep1));
   return RG_OK;
@@ -395,103 +422,48 @@ int ensure_scratch(rg_waveguide* w, size_t bytes) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-rg::SweepArgs base_args(const rg_waveguide* w) {
+// Launch arguments for items of this one waveguide (the caller sets nreal,
+// seeds or upot, outputs and the workspace).
+rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
   rg::SweepArgs a{};
-  a.M = w->nmu;
-  a.ny = w->ny;
-  a.nx = w->nx;
-  a.nxdiso = w->p.nxdiso;
-  a.nxfree = w->p.nxfree;
-  a.row0 = w->imin - 1;
-  a.nrow = w->imax - w->imin + 1;
-  a.col0 = w->jmin - 1;
-  a.ncol = w->jmax - w->jmin + 1;
-  a.neigv = w->neigv;
-  a.mode = rg::kModeEig;
-  a.bmat = w->d_bmat;
-  a.adiag_edge = w->d_aedge;
-  a.adiag_bulk = w->d_abulk;
-  a.sqmu = w->d_sqmu_c;
-  a.costab = w->d_costab;
-  a.expfac = w->d_expfac;
-  a.periodic = w->p.boundtype == RG_BOUND_PERIODIC;
+  a.mode = mode;
+  a.wgs = w->d_desc;
   a.work_counter = w->d_counter;
+  a.max_M = w->nmu;
+  a.max_ny = w->ny;
   return a;
 }
 
-// Largest number of realizations whose potentials are held at once.
-int potential_chunk(const rg_waveguide* w, int n) {
-  const size_t per = sizeof(double) * (size_t)w->p.nxdiso * w->ny;
-  size_t free_b = 0, total_b = 0;
-  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)8 << 30;
-  size_t budget = std::min((size_t)48 << 30, free_b / 2);
-  long long c = (long long)(budget / std::max<size_t>(per, 1));
-  if (c < 1) c = 1;
-  return (int)std::min<long long>(c, n);
+// Plans a launch, grows the scratch to hold `off` bytes plus the per-CTA
+// workspace, and sets a.work.  Pointers into the scratch below `off` must be
+// taken after this call (the scratch may move).
+int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
+  int64_t stride = 0;
+  int rc = rg::sweep_plan(a, w->sm_count, grid, &stride);
+  if (rc) return rc;
+  if ((rc = ensure_scratch(w, off + sizeof(double2) * (size_t)stride * (*grid)))) return rc;
+  a.work = (double2*)((char*)w->d_scratch + off);
+  a.work_stride = stride;
+  return RG_OK;
 }
 
-bool large_modes(const rg_waveguide* w) { return w->nmu > rg::kMaxModesSmem; }
-
-// Seed-driven batch on device buffers.  Up to 64 modes: potentials are drawn
-// chunk by chunk into scratch, then swept.  More modes: one launch of the
-// large-mode kernel, which draws the potential slice by slice itself and
-// needs only its per-CTA workspace.  d_seeds, d_teig, d_status are device
-// pointers.
+// Seed-driven batch on device buffers: one persistent launch, the potential
+// of every item drawn inside the kernel.  d_seeds, d_teig, d_status are
+// device pointers.  CUDA events bracket the launch for rg_last_sweep_time.
 int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_teig, int32_t* d_status,
                    cudaStream_t s) {
-  int rc;
-  if (large_modes(w)) {
-    rg::SweepArgs a = base_args(w);
-    a.nreal = n;
-    a.upot = nullptr;
-    a.seeds = d_seeds;
-    a.jumppoly = w->d_jump;
-    a.stdu = w->stdu;
-    a.teig = d_teig;
-    a.status = d_status;
-    int grid = 0;
-    int64_t stride = 0;
-    if ((rc = rg::sweep_large_plan(a, w->sm_count, &grid, &stride))) return rc;
-    if ((rc = ensure_scratch(w, sizeof(double2) * (size_t)stride * grid))) return rc;
-    a.work = (double2*)w->d_scratch;
-    a.work_stride = stride;
-    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
-    RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
-    if ((rc = rg::launch_sweep_large(a, s, grid))) return rc;
-    RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
-    w->sweep_timed = true;
-    return RG_OK;
-  }
-  const int chunk = potential_chunk(w, n);
-  const size_t pot_bytes = sizeof(double) * (size_t)w->p.nxdiso * w->ny * chunk;
-  rc = ensure_scratch(w, align256(pot_bytes));
-  if (rc) return rc;
-  double* d_pot = (double*)w->d_scratch;
-  for (int k0 = 0; k0 < n; k0 += chunk) {
-    const int nk = std::min(chunk, n - k0);
-    rg::PotArgs pa{};
-    pa.nxdiso = w->p.nxdiso;
-    pa.ny = w->ny;
-    pa.nreal = nk;
-    pa.stdu = w->stdu;
-    pa.seeds = d_seeds + k0;
-    pa.jumppoly = w->d_jump;
-    pa.upot = d_pot;
-    if ((rc = rg::launch_potential(pa, s))) return rc;
-    rg::SweepArgs a = base_args(w);
-    a.nreal = nk;
-    a.upot = d_pot;
-    a.pot_rstride = (int64_t)w->p.nxdiso * w->ny;
-    a.pot_xstride = w->ny;
-    a.pot_ystride = 1;
-    a.teig = d_teig + (int64_t)k0 * w->neigv;
-    a.status = d_status + k0;
-    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
-    if (k0 == 0) RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
-    if ((rc = rg::launch_sweep(a, s, w->sm_count))) return rc;
-  }
+  rg::SweepArgs a = make_args(w, rg::kModeEig);
+  a.nreal = n;
+  a.seeds = d_seeds;
+  a.teig = d_teig;
+  a.status = d_status;
+  int grid = 0, rc;
+  if ((rc = place_workspace(w, a, 0, &grid))) return rc;
+  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
+  if ((rc = rg::launch_sweep(a, s, grid))) return rc;
   RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
-  w->sweep_timed = chunk >= n;  // one sweep launch: the events bracket exactly it
+  w->sweep_timed = true;
   return RG_OK;
 }
 
@@ -509,38 +481,25 @@ const char* status_text(int code) {
   }
 }
 
-// Single realization with either a seed or a host potential; mode selects
-// the eigenvalue path (tdistrib) or the full-t path (v1).  The scratch is
-// laid out once for the whole call: [potential | t | eigenvalues | status |
-// seed | large-mode workspace].
+// Single realization with either a seed (drawn in the kernel) or a host
+// potential; mode selects the eigenvalue path (tdistrib) or the full-t path
+// (v1).  Scratch layout: [potential | t | eigenvalues | status | seed |
+// per-CTA workspace].
 int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int mode, double* h_teig,
                double* h_t, double* h_tfilt) {
   DeviceGuard g(w->device);
   const int M = w->nmu;
-  const bool large = large_modes(w);
-  const bool draw_in_kernel = large && seed != nullptr;
-  const size_t pot = draw_in_kernel ? 0 : sizeof(double) * (size_t)w->p.nxdiso * w->ny;
+  const size_t pot = seed ? 0 : sizeof(double) * (size_t)w->p.nxdiso * w->ny;
   const int nrow = mode == rg::kModeEig ? w->imax - w->imin + 1 : M;
   const int ncol = mode == rg::kModeEig ? w->jmax - w->jmin + 1 : M;
   const size_t tbytes = sizeof(double2) * (size_t)nrow * ncol;
   const size_t off_t = align256(pot), off_e = off_t + align256(tbytes);
   const size_t off_s = off_e + align256(sizeof(double) * w->neigv), off_seed = off_s + 256;
   const size_t off_ws = off_seed + 256;
-
-  rg::SweepArgs a = base_args(w);
+  rg::SweepArgs a = make_args(w, mode);
   a.nreal = 1;
-  a.mode = mode;
-  if (mode == rg::kModeTmat) {
-    a.row0 = 0;
-    a.nrow = M;
-    a.col0 = 0;
-    a.ncol = M;
-    a.sqmu = w->d_sqmu_r;
-  }
   int grid = 1, rc;
-  int64_t stride = 0;
-  if (large && (rc = rg::sweep_large_plan(a, w->sm_count, &grid, &stride))) return rc;
-  if ((rc = ensure_scratch(w, off_ws + (large ? sizeof(double2) * (size_t)stride * grid : 0)))) return rc;
+  if ((rc = place_workspace(w, a, off_ws, &grid))) return rc;
   char* base = (char*)w->d_scratch;
   double* d_pot = (double*)base;
   double2* d_t = (double2*)(base + off_t);
@@ -548,31 +507,14 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
   int32_t* d_status = (int32_t*)(base + off_s);
   int32_t* d_seed = (int32_t*)(base + off_seed);
   cudaStream_t s = w->stream;
-  a.upot = d_pot;
-  a.pot_rstride = 0;
   if (seed) {
     RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    if (draw_in_kernel) {
-      a.upot = nullptr;
-      a.seeds = d_seed;
-      a.jumppoly = w->d_jump;
-      a.stdu = w->stdu;
-    } else {
-      rg::PotArgs pa{};
-      pa.nxdiso = w->p.nxdiso;
-      pa.ny = w->ny;
-      pa.nreal = 1;
-      pa.stdu = w->stdu;
-      pa.seeds = d_seed;
-      pa.jumppoly = w->d_jump;
-      pa.upot = d_pot;
-      if ((rc = rg::launch_potential(pa, s))) return rc;
-      a.pot_xstride = w->ny;
-      a.pot_ystride = 1;
-    }
+    a.seeds = d_seed;
   } else {
     // caller layout upot(nxdiso, ny), x fastest
     RG_CUDA(cudaMemcpyAsync(d_pot, h_upot, pot, cudaMemcpyHostToDevice, s));
+    a.upot = d_pot;
+    a.pot_rstride = 0;
     a.pot_xstride = 1;
     a.pot_ystride = w->p.nxdiso;
   }
@@ -580,13 +522,7 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
   a.teig = d_teig;
   a.status = d_status;
   RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
-  if (large) {
-    a.work = (double2*)(base + off_ws);
-    a.work_stride = stride;
-    if ((rc = rg::launch_sweep_large(a, s, grid))) return rc;
-  } else if ((rc = rg::launch_sweep(a, s, w->sm_count))) {
-    return rc;
-  }
+  if ((rc = rg::launch_sweep(a, s, grid))) return rc;
   int32_t st = 0;
   RG_CUDA(cudaMemcpyAsync(&st, d_status, sizeof st, cudaMemcpyDeviceToHost, s));
   if (h_teig) RG_CUDA(cudaMemcpyAsync(h_teig, d_teig, sizeof(double) * w->neigv, cudaMemcpyDeviceToHost, s));
@@ -607,10 +543,11 @@ int noalloc_view(const rg_waveguide* w, NoAllocView* out) {
   out->sm_count = w->sm_count;
   out->nxdiso = w->p.nxdiso;
   out->ny = w->ny;
+  out->nmu = w->nmu;
   out->stdu = w->stdu;
   out->jumppoly = w->d_jump;
   out->stream = w->stream;
-  out->sweep = base_args(w);
+  out->d_desc = w->d_desc;
   return RG_OK;
 }
 
@@ -804,6 +741,118 @@ int rg_tdistrib_batch(rg_waveguide* w, const int32_t* seeds, int n, double* tall
   if (rc) return rc;
   if (status) std::memcpy(status, st_host.data(), sizeof(int32_t) * n);
   const int bad = first_bad_status(st_host.data(), n);
+  if (bad) return rg::fail(bad, status_text(bad));
+  return RG_OK;
+}
+
+int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, const int64_t* offsets,
+                      double* tallvals, int64_t len, int32_t* status) {
+  if (n < 0 || (n > 0 && (!wgs || !seeds || !offsets || !tallvals)))
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: invalid argument");
+  if (n == 0) return RG_OK;
+  rg_waveguide* w0 = wgs[0];
+  if (!w0) return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: NULL waveguide");
+  // Distinct waveguides, output ranges, and kernel classes.
+  std::vector<rg::WgDesc> descs;
+  std::vector<const rg_waveguide*> uniq;
+  std::vector<int32_t> item_wg(n);
+  for (int k = 0; k < n; ++k) {
+    const rg_waveguide* w = wgs[k];
+    if (!w) return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: NULL waveguide");
+    if (w->device != w0->device) return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: waveguides on different devices");
+    if (offsets[k] < 0 || offsets[k] + w->neigv > len)
+      return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: output range of item " + std::to_string(k) +
+                                              " outside tallvals");
+    size_t u = 0;
+    while (u < uniq.size() && uniq[u] != w) ++u;
+    if (u == uniq.size()) {
+      uniq.push_back(w);
+      descs.push_back(w->h_desc);
+    }
+    item_wg[k] = (int32_t)u;
+  }
+  auto klass = [](int M) { return M <= 16 ? 0 : M <= 32 ? 1 : M <= rg::kMaxModesSmem ? 2 : 3; };
+  // Order: by class (largest first), then by decreasing cost M^3 * nx inside a class.
+  std::vector<int> order(n);
+  for (int k = 0; k < n; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const rg::WgDesc& a = descs[item_wg[x]];
+    const rg::WgDesc& b = descs[item_wg[y]];
+    if (klass(a.M) != klass(b.M)) return klass(a.M) > klass(b.M);
+    return (double)a.M * a.M * a.M * a.nx > (double)b.M * b.M * b.M * b.nx;
+  });
+  std::vector<int32_t> o_wg(n), o_seed(n);
+  std::vector<int64_t> o_off(n);
+  for (int k = 0; k < n; ++k) {
+    o_wg[k] = item_wg[order[k]];
+    o_seed[k] = seeds[order[k]];
+    o_off[k] = offsets[order[k]];
+  }
+  DeviceGuard g(w0->device);
+  cudaStream_t s = w0->stream;
+  const size_t b_desc = align256(sizeof(rg::WgDesc) * descs.size()), b_i32 = align256(sizeof(int32_t) * n);
+  const size_t b_off = align256(sizeof(int64_t) * n), b_out = align256(sizeof(double) * (size_t)len);
+  char* dbuf = nullptr;
+  RG_CUDA(cudaMalloc((void**)&dbuf, b_desc + 3 * b_i32 + b_off + b_out));
+  rg::WgDesc* d_desc = (rg::WgDesc*)dbuf;
+  int32_t* d_wg = (int32_t*)(dbuf + b_desc);
+  int32_t* d_seed = (int32_t*)(dbuf + b_desc + b_i32);
+  int32_t* d_st = (int32_t*)(dbuf + b_desc + 2 * b_i32);
+  int64_t* d_off = (int64_t*)(dbuf + b_desc + 3 * b_i32);
+  double* d_out = (double*)(dbuf + b_desc + 3 * b_i32 + b_off);
+  std::vector<int32_t> st_sorted(n);
+  int rc = RG_OK;
+  cudaError_t e = cudaMemcpyAsync(d_desc, descs.data(), sizeof(rg::WgDesc) * descs.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_wg, o_wg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seed, o_seed.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, o_off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)len, s);
+  if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi upload");
+  // One persistent launch per kernel class.
+  for (int k0 = 0; !rc && k0 < n;) {
+    const int cl = klass(descs[o_wg[k0]].M);
+    int k1 = k0, maxM = 0, maxny = 0;
+    while (k1 < n && klass(descs[o_wg[k1]].M) == cl) {
+      maxM = std::max(maxM, descs[o_wg[k1]].M);
+      maxny = std::max(maxny, descs[o_wg[k1]].ny);
+      ++k1;
+    }
+    rg::SweepArgs a{};
+    a.mode = rg::kModeEig;
+    a.nreal = k1 - k0;
+    a.wgs = d_desc;
+    a.item_wg = d_wg + k0;
+    a.seeds = d_seed + k0;
+    a.teig_off = d_off + k0;
+    a.teig = d_out;
+    a.status = d_st + k0;
+    a.work_counter = w0->d_counter;
+    a.max_M = maxM;
+    a.max_ny = maxny;
+    int grid = 0;
+    if ((rc = place_workspace(w0, a, 0, &grid))) break;
+    e = cudaMemsetAsync(w0->d_counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) {
+      rc = rg::cuda_fail(e, "rg_tdistrib_multi counter");
+      break;
+    }
+    if ((rc = rg::launch_sweep(a, s, grid))) break;
+    k0 = k1;
+  }
+  if (!rc) {
+    e = cudaMemcpyAsync(tallvals, d_out, sizeof(double) * (size_t)len, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st_sorted.data(), d_st, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi");
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(dbuf);
+  if (rc) return rc;
+  int bad = RG_OK;
+  for (int k = 0; k < n; ++k) {
+    if (status) status[order[k]] = st_sorted[k];
+    if (!bad && st_sorted[k] != RG_OK) bad = st_sorted[k];
+  }
   if (bad) return rg::fail(bad, status_text(bad));
   return RG_OK;
 }

@@ -210,3 +210,27 @@ def test_large_batch_matches_single():
         one = np.zeros(s * g.neigv)
         g.compute_tdistrib(int(s), one)
         np.testing.assert_array_equal(b[k * g.neigv:(k + 1) * g.neigv], one[(s - 1) * g.neigv:])
+
+
+def test_multi_uneven_matches_single_and_oracle():
+    """Uneven sizes in one call (kernel classes 16/32/64/large mixed, absorption on some)."""
+    specs = [
+        dict(boundtype="dirichlet", nxdiso=50, nxfree=0, wol=5.25, exfac=1.0, dscat=3.0, ny=40),
+        dict(boundtype="dirichlet", nxdiso=80, nxfree=0, wol=10.25, exfac=1.0, dscat=6.0, ny=80, dabso=0.3),
+        dict(boundtype="dirichlet", nxdiso=60, nxfree=1, wol=20.25, exfac=1.0, dscat=9.0, ny=160),
+        dict(boundtype="periodic", nxdiso=40, nxfree=0, wol=12.3, exfac=1.0, dscat=2.0),
+        dict(boundtype="dirichlet", nxdiso=20, nxfree=0, wol=36.25, exfac=1.0, dscat=4.0, ny=144, dabso=0.8),
+        dict(boundtype="dirichlet", nxdiso=10, nxfree=0, wol=50.25, exfac=1.0, dscat=12.0, ny=200),
+    ]
+    gs = [rg.Waveguide(**kw) for kw in specs]
+    items = [(gs[k % len(gs)], 1 + k) for k in range(18)]
+    res, st = rg.tdistrib_multi(items, return_status=True)
+    assert np.all(st == 0)
+    for (g, s), T in zip(items, res):
+        one = np.zeros(s * g.neigv)
+        g.compute_tdistrib(s, one)
+        np.testing.assert_array_equal(T, one[(s - 1) * g.neigv:])
+    for k in (0, 3, 4, 5):
+        o = O.Waveguide(**specs[k])
+        g, s = items[k]
+        assert np.max(np.abs(res[k] - o.tdistrib_upot(o.potential(s)))) <= TN_ABS
