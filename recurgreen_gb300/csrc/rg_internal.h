@@ -69,6 +69,7 @@ struct SweepArgs {
   double2* work;              // per-CTA workspace in global memory
   int64_t work_stride;        // double2 elements per CTA
   int max_M, max_ny;          // largest M and ny among the items (shared-memory sizing)
+  int cluster;                // CTAs per work item (large-mode kernel; set by sweep_plan)
 };
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
@@ -87,10 +88,10 @@ struct PotArgs {
 // size and per-CTA workspace, from max_M/max_ny and the kernel's occupancy),
 // then launched with a.work pointing at grid * work_stride double2 elements.
 int launch_potential(const PotArgs& a, cudaStream_t stream);
-int sweep_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid);
 // The large-mode kernel behind sweep_plan/launch_sweep for max_M > kMaxModesSmem (rg_sweep_large.cu).
-int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
                      unsigned long long* d_counts, cudaStream_t stream);

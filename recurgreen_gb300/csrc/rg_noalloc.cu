@@ -83,7 +83,7 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   const bool large = v.nmu > rg::kMaxModesSmem;
   const size_t pot_doubles = (size_t)v.nxdiso * (size_t)v.ny;
   const size_t pot_bytes = (pot_doubles * sizeof(double) + 255) & ~(size_t)255;
-  const size_t ws_bytes = large ? sizeof(double2) * (size_t)stride * grid : 0;
+  const size_t ws_bytes = large ? sizeof(double2) * (size_t)stride * (grid / a.cluster) : 0;
   if (pot_bytes + ws_bytes > kNoAllocScratchBytes - kNoAllocHeaderBytes)
     return rg::fail(RG_ERR_INVALID_ARG,
                     "rg_tdistrib_seed_noalloc: nxdiso*ny = " + std::to_string(pot_doubles) +

@@ -500,7 +500,8 @@ __global__ void histogram_kernel(const double* __restrict__ x, int64_t n, const 
 }
 
 template <int MCAP, int NT, int MINB>
-int plan_t(const SweepArgs& a, int sm_count, int* grid, int64_t* stride) {
+int plan_t(SweepArgs& a, int sm_count, int* grid, int64_t* stride) {
+  a.cluster = 1;
   const size_t smem = SweepSmem<MCAP>::bytes(a.max_ny);
   RG_CUDA(cudaFuncSetAttribute(sweep_kernel<MCAP, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -530,7 +531,7 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
   return RG_OK;
 }
 
-int sweep_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
   if (a.max_M <= 16) return plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
   if (a.max_M <= 32) return plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
   if (a.max_M <= kMaxModesSmem) return plan_t<64, 256, 2>(a, sm_count, grid, work_stride);

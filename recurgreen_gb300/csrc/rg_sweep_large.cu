@@ -1,6 +1,6 @@
 // Recursive Green sweep for many modes (M > 64): the slice matrices no longer
 // fit in shared memory, so W (the slice matrix inverted in place) and R (the
-// propagator right-hand side) live in a per-CTA workspace in global memory
+// propagator right-hand side) live in a workspace in global memory
 // (L2-resident when the batch allows), and Gauss-Jordan runs blocked:
 //
 //   for each panel of NB columns
@@ -19,30 +19,48 @@
 // 1/NB of the unblocked elimination.  The disorder is drawn in-kernel, one
 // xoshiro256** state per transverse column kept in the workspace, so the
 // Nx x ny potential of a large guide never goes through HBM.
+//
+// A work item can be spread over a thread-block cluster of C CTAs (C SMs).
+// Every CTA of the cluster factors each panel itself (same input, same code,
+// same result, so no pivot data is exchanged), the rank-NB update, slice
+// assembly, disorder draws and eigenvalue rotations are split across the
+// CTAs, and a cluster barrier separates the phases.  Data another CTA wrote
+// is read with ld.global.cg (L2, never a stale L1 line).
+#include <cooperative_groups.h>
+
 #include "rg_device.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace rg {
 namespace {
 
 constexpr int kLargeNT = 256;
 constexpr int kLargeNB = 8;
+constexpr int kMaxCluster = 8;
+constexpr int kMaxRowSplit = 8;  // threads sharing one column's rows in the rank-NB update
 
 struct LargeSmem {
   static size_t bytes(int M, int ny) {
     const int nyp = (ny + 1) & ~1;
-    return sizeof(double2) * (2 * (size_t)M * kLargeNB + kLargeNB * kLargeNB + M + kLargeNB) +
+    return sizeof(double2) * (2 * (size_t)M * kLargeNB + kLargeNB * kLargeNB + M + kLargeNB +
+                               (kLargeNT / 2) * kLargeNB) +
            sizeof(double) * (2 * M + 2 + nyp) + sizeof(int) * 5 * M;
   }
 };
 
-// Workspace of one CTA, in double2 units: W (two buffers), R, t, generator states.
+// Workspace of one cluster, in double2 units: W (two buffers), R, t,
+// generator states (ny x 4 uint64) and the drawn potential row (ny doubles).
 inline int64_t large_stride(int M, int ny) {
   const int64_t mm = (int64_t)M * M;
-  return ((4 * mm + 2 * (int64_t)ny) + 15) & ~(int64_t)15;
+  return ((4 * mm + 2 * (int64_t)ny + (ny + 1) / 2) + 15) & ~(int64_t)15;
 }
 
 __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
   constexpr int NT = kLargeNT, NB = kLargeNB, NW = NT / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
   const int MX = a.max_M;
   extern __shared__ double2 sm[];
   double2* P = sm;                          // [M][NB] current panel
@@ -50,7 +68,8 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
   double2* Lt = Ub + MX * NB;               // [NB][NB] Lt[k][l] = u_l[p_k], l < k
   double2* colf = Lt + NB * NB;             // [M] panel column before the step
   double2* rowp = colf + MX;                // [NB] scaled pivot row inside the panel
-  double* cc = (double*)(rowp + NB);        // [2M+2] projection coefficients
+  double2* zsh = rowp + NB;                 // [NT/2][NB] z of the columns of a chunk (row split)
+  double* cc = (double*)(zsh + (NT / 2) * NB);  // [2M+2] projection coefficients
   double* urow = cc + (2 * MX + 2);         // [ny] potential of the slice
   int* piv = (int*)(urow + ((a.max_ny + 1) & ~1));
   int* pinv = piv + MX;
@@ -64,33 +83,40 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
   __shared__ WgDesc wd;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ctid = rank * NT + tid, CNT = C * NT;  // thread index and count in the cluster
   const bool draw = (a.upot == nullptr);
   const bool tmat = (a.mode == kModeTmat);
 
   for (;;) {
-    if (tid == 0) {
+    if (rank == 0 && tid == 0) {
       s_r = atomicAdd(a.work_counter, 1);
       if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
     }
-    __syncthreads();
+    cluster.sync();
+    if (rank != 0 && tid == 0) {
+      s_r = *cluster.map_shared_rank(&s_r, 0);
+      if (s_r < a.nreal) wd = *cluster.map_shared_rank(&wd, 0);
+    }
+    cluster.sync();  // rank 0's shared memory has been read before any CTA can leave the loop
     const int r = s_r;
     if (r >= a.nreal) break;
     const int M = wd.M, ny = wd.ny;
     const int64_t mm = (int64_t)M * M;
-    double2* ws = a.work + (int64_t)blockIdx.x * a.work_stride;
+    double2* ws = a.work + (int64_t)(blockIdx.x / C) * a.work_stride;
     double2* const Wb0 = ws;
     double2* const Wb1 = ws + mm;
     double2* Rg = ws + 2 * mm;
     double2* Tg = ws + 3 * mm;
-    uint64_t* gen = (uint64_t*)(ws + 4 * mm);  // [ny][4]
+    uint64_t* gen = (uint64_t*)(ws + 4 * mm);     // [ny][4]
+    double* urow_g = (double*)(gen + 4 * ny);     // [ny] drawn row, shared by the cluster
     if (tid == 0) s_status = RG_OK;
     for (int c = tid; c < M; c += NT) {
       sinv[c] = c;
       used[c] = 0;
     }
-    for (int64_t e = tid; e < mm; e += NT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
     if (draw) {
-      for (int iy = tid; iy < ny; iy += NT) {
+      for (int iy = ctid; iy < ny; iy += CNT) {
         const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
         gen[4 * iy + 0] = st.s0;
         gen[4 * iy + 1] = st.s1;
@@ -99,7 +125,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       }
     }
     const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;
-    __syncthreads();
+    cluster.sync();
 
     int cur = 0;
     for (int n = 0; n < wd.nx; ++n) {
@@ -108,14 +134,16 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       if (dis) {
         // 1. This slice's potential row (drawn or loaded) and its projection.
         if (draw) {
-          for (int iy = tid; iy < ny; iy += NT) {
+          for (int iy = ctid; iy < ny; iy += CNT) {
             Xoshiro st{gen[4 * iy], gen[4 * iy + 1], gen[4 * iy + 2], gen[4 * iy + 3]};
-            urow[iy] = scaled_normal(wd.stdu, st);
+            urow_g[iy] = scaled_normal(wd.stdu, st);
             gen[4 * iy + 0] = st.s0;
             gen[4 * iy + 1] = st.s1;
             gen[4 * iy + 2] = st.s2;
             gen[4 * iy + 3] = st.s3;
           }
+          cluster.sync();
+          for (int j = tid; j < ny; j += NT) urow[j] = __ldcg(urow_g + j);
         } else {
           for (int j = tid; j < ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
         }
@@ -152,13 +180,13 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       }
 
       // 2. Assemble X = A_n - V_n - B Gss B (physical row order) into the
-      //    other W buffer, and R = B Gs1 in place.
+      //    other W buffer, and R = B Gs1 in place (elements split over the cluster).
       double2* Wold = cur ? Wb1 : Wb0;
       double2* W = cur ? Wb0 : Wb1;
       cur ^= 1;
       const double2* adiag = (n == 0 || n == wd.nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
       const double rsign = (n == 1) ? 1.0 : -1.0;
-      for (int64_t e = tid; e < mm; e += NT) {
+      for (int64_t e = ctid; e < mm; e += CNT) {
         const int q = (int)(e / M), c = (int)(e % M);
         const int al = (n == 0) ? q : pinv[q];
         double2 x = (al == c) ? adiag[c] : make_double2(0.0, 0.0);
@@ -174,19 +202,19 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           x = csub(x, vac);
         }
         if (n > 0) {
-          x = csub(x, cmul(cmul(wd.bmat[al], Wold[(int64_t)q * M + colmap[c]]), wd.bmat[c]));
-          Rg[e] = cmul(wd.bmat[al], cscale(rsign, Rg[e]));
+          x = csub(x, cmul(cmul(wd.bmat[al], __ldcg(Wold + (int64_t)q * M + colmap[c])), wd.bmat[c]));
+          Rg[e] = cmul(wd.bmat[al], cscale(rsign, __ldcg(Rg + e)));
         }
         W[e] = x;
       }
-      __syncthreads();
+      cluster.sync();
 
       // 3. Blocked Gauss-Jordan with implicit partial pivoting.
       for (int k0 = 0; k0 < M; k0 += NB) {
         const int nbk = min(NB, M - k0);
         for (int e = tid; e < M * nbk; e += NT) {
           const int i = e / nbk, l = e % nbk;
-          P[i * NB + l] = W[(int64_t)i * M + k0 + l];
+          P[i * NB + l] = __ldcg(W + (int64_t)i * M + k0 + l);
         }
         __syncthreads();
         for (int kk = 0; kk < nbk; ++kk) {
@@ -273,51 +301,80 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
           Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
         }
         __syncthreads();
-        // d. the panel's steps applied to every other column of [W | R]
+        // d. the panel's steps applied to every other column of [W | R].
+        //    Columns are dealt round-robin to the cluster's CTAs (jj = rank +
+        //    C*c); when a CTA has fewer columns than threads, T threads share
+        //    a column's rows and its z comes through shared memory.
         const int ntrail = 2 * M - nbk;
-        for (int jj = tid; jj < ntrail; jj += NT) {
+        const int ncl = (ntrail - rank + C - 1) / C;
+        int T = 1;
+        while (T < kMaxRowSplit && ncl * T * 2 <= NT) T *= 2;
+        const int NCH = NT / T;  // columns per chunk
+        const int cs = tid % NCH, sub = tid / NCH;
+        for (int c0 = 0; c0 < ncl; c0 += NCH) {
+          const int c = c0 + cs;
+          const bool active = c < ncl;
+          const int jj = rank + C * c;
           const int j = jj < k0 ? jj : jj + nbk;
-          double2* col = (j < M) ? W + j : Rg + (j - M);
+          double2* col = active ? ((j < M) ? W + j : Rg + (j - M)) : nullptr;
           double2 z[NB];
 #pragma unroll
-          for (int k = 0; k < NB; ++k) {
-            z[k] = make_double2(0.0, 0.0);
-            if (k < nbk) {
-              double2 v = col[(int64_t)piv[k0 + k] * M];
+          for (int k = 0; k < NB; ++k) z[k] = make_double2(0.0, 0.0);
+          if (active && sub == 0) {
 #pragma unroll
-              for (int l = 0; l < k; ++l) v = cfms(v, make_double2(-Lt[k * NB + l].x, -Lt[k * NB + l].y), z[l]);
-              z[k] = v;
+            for (int k = 0; k < NB; ++k) {
+              if (k < nbk) {
+                double2 v = __ldcg(col + (int64_t)piv[k0 + k] * M);
+#pragma unroll
+                for (int l = 0; l < k; ++l) v = cfms(v, make_double2(-Lt[k * NB + l].x, -Lt[k * NB + l].y), z[l]);
+                z[k] = v;
+              }
+            }
+            if (T > 1) {
+#pragma unroll
+              for (int k = 0; k < NB; ++k) zsh[cs * NB + k] = z[k];
             }
           }
-          if (nbk == NB) {
-            for (int i = 0; i < M; ++i) {
-              double2 x = col[(int64_t)i * M];
-              const double2* ui = Ub + i * NB;
+          if (T > 1) {
+            __syncthreads();  // z is read before any pivot row of these columns changes
+            if (active) {
 #pragma unroll
-              for (int k = 0; k < NB; ++k) {
-                const double2 u = ui[k];
-                x = cfms(x, make_double2(-u.x, -u.y), z[k]);
-              }
-              col[(int64_t)i * M] = x;
-            }
-          } else {
-            for (int i = 0; i < M; ++i) {
-              double2 x = col[(int64_t)i * M];
-              const double2* ui = Ub + i * NB;
-              for (int k = 0; k < nbk; ++k) {
-                const double2 u = ui[k];
-                x = cfms(x, make_double2(-u.x, -u.y), z[k]);
-              }
-              col[(int64_t)i * M] = x;
+              for (int k = 0; k < NB; ++k) z[k] = zsh[cs * NB + k];
             }
           }
+          if (active) {
+            if (nbk == NB) {
+              for (int i = sub; i < M; i += T) {
+                double2 x = __ldcg(col + (int64_t)i * M);
+                const double2* ui = Ub + i * NB;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                  const double2 u = ui[k];
+                  x = cfms(x, make_double2(-u.x, -u.y), z[k]);
+                }
+                col[(int64_t)i * M] = x;
+              }
+            } else {
+              for (int i = sub; i < M; i += T) {
+                double2 x = __ldcg(col + (int64_t)i * M);
+                const double2* ui = Ub + i * NB;
+                for (int k = 0; k < nbk; ++k) {
+                  const double2 u = ui[k];
+                  x = cfms(x, make_double2(-u.x, -u.y), z[k]);
+                }
+                col[(int64_t)i * M] = x;
+              }
+            }
+          }
+          if (T > 1) __syncthreads();  // zsh is reused by the next chunk
         }
-        __syncthreads();
-        for (int e = tid; e < M * nbk; e += NT) {
-          const int i = e / nbk, l = e % nbk;
-          W[(int64_t)i * M + k0 + l] = P[i * NB + l];
+        if (rank == 0) {
+          for (int e = tid; e < M * nbk; e += NT) {
+            const int i = e / nbk, l = e % nbk;
+            W[(int64_t)i * M + k0 + l] = P[i * NB + l];
+          }
         }
-        __syncthreads();
+        cluster.sync();
       }
 
       // 4. Permutation bookkeeping for the next slice.
@@ -337,20 +394,21 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
     const int nrow = tmat ? M : wd.nrow, ncol = tmat ? M : wd.ncol;
     const double2* sqmu = tmat ? wd.sqmu_r : wd.sqmu_c;
     double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
-    for (int e = tid; e < nrow * ncol; e += NT) {
+    for (int e = ctid; e < nrow * ncol; e += CNT) {
       const int i = e % nrow, j = e / nrow;
       const int gi = row0 + i, gj = col0 + j;
-      const double2 g = cscale(gsign, Rg[(int64_t)piv[gi] * M + gj]);
+      const double2 g = cscale(gsign, __ldcg(Rg + (int64_t)piv[gi] * M + gj));
       const double2 v = cmul(cmul(sqmu[gi], g), sqmu[gj]);
       const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);
       Tg[e] = t;
       if (tout) tout[e] = t;
     }
-    __syncthreads();
+    cluster.sync();
 
     if (!tmat) {
       // 6. Eigenvalues of t^H t: one-sided Jacobi on the vectors of the
-      //    smaller dimension (columns of t, or its rows), in the workspace.
+      //    smaller dimension (columns of t, or its rows), in the workspace;
+      //    the pairs of a round are split over the cluster's warps.
       const bool bycol = nrow >= ncol;
       const int nv = bycol ? ncol : nrow;
       const int L = bycol ? nrow : ncol;
@@ -358,12 +416,13 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       const int vs = bycol ? nrow : 1;
       const int NP = (nv + 1) & ~1;
       const double tol = 2.220446049250313e-16 * L;
+      int* rot0 = cluster.map_shared_rank(&s_rot, 0);
       int sweep = 0;
       for (; sweep < 60; ++sweep) {
-        if (tid == 0) s_rot = 0;
-        __syncthreads();
+        if (rank == 0 && tid == 0) s_rot = 0;
+        cluster.sync();
         for (int rr = 0; rr < NP - 1; ++rr) {
-          for (int pk = warp; pk < NP / 2; pk += NW) {
+          for (int pk = rank * NW + warp; pk < NP / 2; pk += C * NW) {
             const int pos1 = pk, pos2 = NP - 1 - pk;
             const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
             const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
@@ -372,7 +431,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
             double2* xq = Tg + (int64_t)vq * vs;
             double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
             for (int i = lane; i < L; i += 32) {
-              const double2 u = xp[(int64_t)i * es], w = xq[(int64_t)i * es];
+              const double2 u = __ldcg(xp + (int64_t)i * es), w = __ldcg(xq + (int64_t)i * es);
               al = fma(u.x, u.x, fma(u.y, u.y, al));
               be = fma(w.x, w.x, fma(w.y, w.y, be));
               gr = fma(u.x, w.x, fma(u.y, w.y, gr));
@@ -387,67 +446,99 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
             }
             const double ga = sqrt(gr * gr + gi * gi);
             if (ga > tol * sqrt(al * be) && ga > 1e-300) {
-              if (lane == 0) s_rot = 1;
+              if (lane == 0) atomicOr(rot0, 1);
               const double zeta = (be - al) / (2.0 * ga);
               const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
                                                   : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
               const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
               const double2 ph = make_double2(gr / ga, -gi / ga);
               for (int i = lane; i < L; i += 32) {
-                const double2 u = xp[(int64_t)i * es];
-                const double2 w = cmul(ph, xq[(int64_t)i * es]);
+                const double2 u = __ldcg(xp + (int64_t)i * es);
+                const double2 w = cmul(ph, __ldcg(xq + (int64_t)i * es));
                 xp[(int64_t)i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
                 xq[(int64_t)i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
               }
             }
           }
-          __syncthreads();
+          cluster.sync();
         }
-        if (!s_rot) break;
-        __syncthreads();
+        const int any = *rot0;
+        cluster.sync();  // every CTA has read the flag before rank 0 clears it
+        if (!any) break;
       }
       if (sweep == 60 && tid == 0) s_status = RG_ERR_NOCONV;
-      for (int k = warp; k < nv; k += NW) {
-        const double2* xk = Tg + (int64_t)k * vs;
-        double s = 0.0;
-        for (int i = lane; i < L; i += 32) {
-          const double2 u = xk[(int64_t)i * es];
-          s = fma(u.x, u.x, fma(u.y, u.y, s));
-        }
+      if (rank == 0) {
+        for (int k = warp; k < nv; k += NW) {
+          const double2* xk = Tg + (int64_t)k * vs;
+          double s = 0.0;
+          for (int i = lane; i < L; i += 32) {
+            const double2 u = __ldcg(xk + (int64_t)i * es);
+            s = fma(u.x, u.x, fma(u.y, u.y, s));
+          }
 #pragma unroll
-        for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (lane == 0) cc[k] = s;
-      }
-      __syncthreads();
-      const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
-      for (int k = tid; k < nv; k += NT) {
-        const double tk = cc[k];
-        int rank = 0;
-        for (int j = 0; j < nv; ++j) {
-          const double tj = cc[j];
-          rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+          for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+          if (lane == 0) cc[k] = s;
         }
-        if (rank < wd.neigv) a.teig[obase + rank] = tk;
+        __syncthreads();
+        const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
+        for (int k = tid; k < nv; k += NT) {
+          const double tk = cc[k];
+          int rank_k = 0;
+          for (int j = 0; j < nv; ++j) {
+            const double tj = cc[j];
+            rank_k += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+          }
+          if (rank_k < wd.neigv) a.teig[obase + rank_k] = tk;
+        }
       }
     }
     __syncthreads();
-    if (tid == 0) a.status[r] = s_status;
+    if (rank == 0 && tid == 0) a.status[r] = s_status;
+    cluster.sync();  // the cluster finishes this item before rank 0 takes the next
   }
 }
 
 }  // namespace
 
-int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+// Cluster size: spread an item over several SMs when there are fewer items
+// than CTA slots, so a small batch (or one large realization) still fills
+// the GPU; full batches run one CTA per item (no redundant panel work).
+int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
   const size_t smem = LargeSmem::bytes(a.max_M, a.max_ny);
   if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes or transverse points for the large-mode kernel");
   RG_CUDA(cudaFuncSetAttribute(sweep_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_large_kernel, kLargeNT, smem));
   if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "large-mode sweep kernel does not fit on an SM");
-  int g = per_sm * sm_count;
-  if (g > a.nreal) g = a.nreal;
-  if (g < 1) g = 1;
-  *grid = g;
+  const int slots = per_sm * sm_count;
+  int C = 1;
+  while (C < kMaxCluster && (int64_t)a.nreal * C * 2 <= slots) C *= 2;
+  int nclusters = slots / C;
+  if (C > 1) {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = C;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C * 64);
+    cfg.blockDim = dim3(kLargeNT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int maxc = 0;
+    RG_CUDA(cudaOccupancyMaxActiveClusters(&maxc, sweep_large_kernel, &cfg));
+    if (maxc < 1) {
+      C = 1;
+      nclusters = slots;
+    } else {
+      nclusters = maxc;
+    }
+  }
+  if (nclusters > a.nreal) nclusters = a.nreal;
+  if (nclusters < 1) nclusters = 1;
+  a.cluster = C;
+  *grid = nclusters * C;
   *work_stride = large_stride(a.max_M, a.max_ny);
   return RG_OK;
 }
@@ -455,8 +546,20 @@ int sweep_large_plan(const SweepArgs& a, int sm_count, int* grid, int64_t* work_
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
   const size_t smem = LargeSmem::bytes(a.max_M, a.max_ny);
-  sweep_large_kernel<<<grid, kLargeNT, smem, stream>>>(a);
-  RG_CUDA(cudaGetLastError());
+  const int C = a.cluster > 0 ? a.cluster : 1;
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute attr{};
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = C;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kLargeNT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  RG_CUDA(cudaLaunchKernelEx(&cfg, sweep_large_kernel, a));
   return RG_OK;
 }
 

@@ -441,7 +441,8 @@ int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
   int64_t stride = 0;
   int rc = rg::sweep_plan(a, w->sm_count, grid, &stride);
   if (rc) return rc;
-  if ((rc = ensure_scratch(w, off + sizeof(double2) * (size_t)stride * (*grid)))) return rc;
+  const int slots = *grid / (a.cluster > 0 ? a.cluster : 1);  // one workspace per cluster
+  if ((rc = ensure_scratch(w, off + sizeof(double2) * (size_t)stride * slots))) return rc;
   a.work = (double2*)((char*)w->d_scratch + off);
   a.work_stride = stride;
   return RG_OK;
