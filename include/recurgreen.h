@@ -100,7 +100,9 @@ int rg_compute_tdistrib(rg_waveguide* wg, int iseed, double* tallvals, int64_t l
 /* compute_refl_trans_v1 (src/waveguide.f90:469-519): full nmu x nmu
  * transmission matrix t (and, if rmat != NULL, reflection matrix r) of seed
  * iseed, Fisher-Lee with sqrt(real(mu)).  Host buffers of nmu*nmu complex
- * doubles, column-major. */
+ * doubles, column-major.  r comes from a second sweep over the slices in
+ * reverse order (its last Gss is G(x_1; x_1)), instead of the reference's two
+ * extra matrix products per slice. */
 int rg_compute_refl_trans_v1(rg_waveguide* wg, int iseed, double* rmat, double* tmat);
 
 /* As rg_compute_tdistrib / rg_compute_refl_trans_v1, but for a caller-given

@@ -167,11 +167,12 @@ class Waveguide:
             raise RecurGreenError(RG_ERR_INVALID_ARG, "tallvals must be a contiguous float64 array")
         _check(lib().rg_compute_tdistrib(self._h, int(iseed), _dp(tallvals), tallvals.size))
 
-    def compute_refl_trans_v1(self, iseed: int) -> np.ndarray:
-        """t of compute_refl_trans_v1 (src/waveguide.f90:469-519), nmu x nmu complex."""
+    def compute_refl_trans_v1(self, iseed: int):
+        """compute_refl_trans_v1 (src/waveguide.f90:469-519): (r, t), nmu x nmu complex."""
         t = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
-        _check(lib().rg_compute_refl_trans_v1(self._h, int(iseed), None, t.ctypes.data))
-        return t
+        r = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_compute_refl_trans_v1(self._h, int(iseed), r.ctypes.data, t.ctypes.data))
+        return r, t
 
     def tdistrib_upot(self, upot: np.ndarray, want_t: bool = False):
         """Eigenvalues (and the filtered Fisher-Lee t) for a given potential
@@ -184,13 +185,21 @@ class Waveguide:
         _check(lib().rg_tdistrib_upot(self._h, _dp(upot), _dp(T), t.ctypes.data if want_t else None))
         return (T, t) if want_t else T
 
-    def refl_trans_v1_upot(self, upot: np.ndarray) -> np.ndarray:
+    def refl_trans_v1_upot(self, upot: np.ndarray, want_r: bool = False):
+        """t (and r) of compute_refl_trans_v1 for a given potential."""
         upot = np.ascontiguousarray(upot, np.float64)
         if upot.shape != (self.ny, self.nxdiso):
             raise RecurGreenError(RG_ERR_INVALID_ARG, f"upot must have shape {(self.ny, self.nxdiso)}")
         t = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
-        _check(lib().rg_refl_trans_v1_upot(self._h, _dp(upot), None, t.ctypes.data))
-        return t
+        r = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_refl_trans_v1_upot(self._h, _dp(upot), r.ctypes.data if want_r else None, t.ctypes.data))
+        return (r, t) if want_r else t
+
+    def test_unitarity(self, iseed: int) -> float:
+        """test_unitarity (src/waveguide.f90:561-590): ||t^H t + r^H r - 1||."""
+        r, t = self.compute_refl_trans_v1(iseed)
+        d = t.conj().T @ t + r.conj().T @ r - np.eye(self.nmu)
+        return float(np.sqrt(np.sum((d * d.conj()).real)))
 
     def potential(self, iseed: int) -> np.ndarray:
         """The disorder of seed iseed as drawn on the GPU, shape (ny, nxdiso)."""

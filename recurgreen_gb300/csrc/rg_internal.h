@@ -73,7 +73,9 @@ struct SweepArgs {
 };
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
-constexpr int kModeTmat = 1;  // v1 t only: full t written to tout
+constexpr int kModeTmat = 1;  // v1 t: full t written to tout
+constexpr int kModeRefl = 2;  // v1 r: the sweep runs over the slices in reverse order, and
+                              // its last Gss is G(x_1; x_1) of the guide; r goes to tout
 
 // Potential generator arguments.
 struct PotArgs {

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
   uint64_t* gen = (uint64_t*)(a.work + (int64_t)blockIdx.x * a.work_stride);  // [max_ny][4]
   const bool draw = (a.upot == nullptr);
   const bool tmat = (a.mode == kModeTmat);
+  const bool refl = (a.mode == kModeRefl);
   double2 R[AMAX][CB];
 
   for (;;) {
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
     __syncthreads();
 
     for (int n = 0; n < nx; ++n) {
-      const int id = n - wd.nxfree;
+      const int id = (refl ? nx - 1 - n : n) - wd.nxfree;  // slice of the guide swept at step n
       const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
         // 1. This slice's potential row (drawn or loaded) and its projection.
@@ -338,6 +339,21 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
         used[c] = 0;
       }
       __syncthreads();
+    }
+
+    if (refl) {
+      // 5'. Reflection: after the reverse sweep W holds G(x_1; x_1) with
+      //     G11[a][c] = W[piv[a]][colmap[c]];  r = -1 + 2i sqmu_a G11 sqmu_c
+      //     with sqrt(real(mu)) (src/waveguide.f90:510-512).
+      double2* rout = a.tout + (int64_t)r * M * M;
+      for (int e = tid; e < M * M; e += NT) {
+        const int i = e % M, j = e / M;
+        const double2 v = cmul(cmul(wd.sqmu_r[i], W[piv[i] * LDW + colmap[j]]), wd.sqmu_r[j]);
+        rout[e] = make_double2((i == j ? -1.0 : 0.0) - 2.0 * v.y, 2.0 * v.x);
+      }
+      __syncthreads();
+      if (tid == 0) a.status[r] = s_status;
+      continue;
     }
 
     // 5. Fisher-Lee: Gs1[a][j] = sign * R[piv[a]][j]; t = 2i sqmu_a Gs1 sqmu_j.

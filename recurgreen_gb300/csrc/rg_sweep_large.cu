@@ -86,6 +86,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
   const int ctid = rank * NT + tid, CNT = C * NT;  // thread index and count in the cluster
   const bool draw = (a.upot == nullptr);
   const bool tmat = (a.mode == kModeTmat);
+  const bool refl = (a.mode == kModeRefl);
 
   for (;;) {
     if (rank == 0 && tid == 0) {
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
 
     int cur = 0;
     for (int n = 0; n < wd.nx; ++n) {
-      const int id = n - wd.nxfree;
+      const int id = (refl ? wd.nx - 1 - n : n) - wd.nxfree;  // slice of the guide swept at step n
       const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
         // 1. This slice's potential row (drawn or loaded) and its projection.
@@ -385,6 +386,22 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         used[c] = 0;
       }
       __syncthreads();
+    }
+
+    if (refl) {
+      // 5'. Reflection: the reverse sweep's last Gss is G(x_1; x_1):
+      //     G11[a][c] = W[piv[a]][colmap[c]];  r = -1 + 2i sqmu_a G11 sqmu_c.
+      const double2* Wl = cur ? Wb1 : Wb0;  // buffer the last slice was inverted in
+      double2* rout = a.tout + (int64_t)r * M * M;
+      for (int e = ctid; e < M * M; e += CNT) {
+        const int i = e % M, j = e / M;
+        const double2 v = cmul(cmul(wd.sqmu_r[i], __ldcg(Wl + (int64_t)piv[i] * M + colmap[j])), wd.sqmu_r[j]);
+        rout[e] = make_double2((i == j ? -1.0 : 0.0) - 2.0 * v.y, 2.0 * v.x);
+      }
+      __syncthreads();
+      if (rank == 0 && tid == 0) a.status[r] = s_status;
+      cluster.sync();
+      continue;
     }
 
     // 5. Fisher-Lee: t = 2i sqmu_a Gs1 sqmu_j with Gs1[a][j] = sign * R[piv[a]][j];

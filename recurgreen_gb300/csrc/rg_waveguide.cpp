@@ -482,19 +482,25 @@ const char* status_text(int code) {
   }
 }
 
-// Single realization with either a seed (drawn in the kernel) or a host
-// potential; mode selects the eigenvalue path (tdistrib) or the full-t path
-// (v1).  Scratch layout: [potential | t | eigenvalues | status | seed |
-// per-CTA workspace].
+// Single realization with either a seed or a host potential.  mode selects
+// the eigenvalue path (tdistrib) or the v1 path (full t; and r when h_r is
+// given: a second sweep over the slices in reverse order, whose last Gss is
+// G(x_1; x_1)).  The seed's potential is drawn inside the kernel, except for
+// r, whose reverse sweep needs the rows in reverse order: then it is drawn
+// into scratch first.  Scratch layout: [potential | t | r | eigenvalues |
+// status | seed | per-CTA workspace].
 int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int mode, double* h_teig,
-               double* h_t, double* h_tfilt) {
+               double* h_t, double* h_tfilt, double* h_r = nullptr) {
   DeviceGuard g(w->device);
   const int M = w->nmu;
-  const size_t pot = seed ? 0 : sizeof(double) * (size_t)w->p.nxdiso * w->ny;
+  const bool want_r = (h_r != nullptr);
+  const bool materialize = !seed || want_r;
+  const size_t pot = materialize ? sizeof(double) * (size_t)w->p.nxdiso * w->ny : 0;
   const int nrow = mode == rg::kModeEig ? w->imax - w->imin + 1 : M;
   const int ncol = mode == rg::kModeEig ? w->jmax - w->jmin + 1 : M;
   const size_t tbytes = sizeof(double2) * (size_t)nrow * ncol;
-  const size_t off_t = align256(pot), off_e = off_t + align256(tbytes);
+  const size_t rbytes = want_r ? sizeof(double2) * (size_t)M * M : 0;
+  const size_t off_t = align256(pot), off_r = off_t + align256(tbytes), off_e = off_r + align256(rbytes);
   const size_t off_s = off_e + align256(sizeof(double) * w->neigv), off_seed = off_s + 256;
   const size_t off_ws = off_seed + 256;
   rg::SweepArgs a = make_args(w, mode);
@@ -504,33 +510,57 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
   char* base = (char*)w->d_scratch;
   double* d_pot = (double*)base;
   double2* d_t = (double2*)(base + off_t);
+  double2* d_r = (double2*)(base + off_r);
   double* d_teig = (double*)(base + off_e);
   int32_t* d_status = (int32_t*)(base + off_s);
   int32_t* d_seed = (int32_t*)(base + off_seed);
   cudaStream_t s = w->stream;
-  if (seed) {
-    RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  if (seed) RG_CUDA(cudaMemcpyAsync(d_seed, seed, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  if (!materialize) {
     a.seeds = d_seed;
+  } else if (seed) {
+    rg::PotArgs pa{};
+    pa.nxdiso = w->p.nxdiso;
+    pa.ny = w->ny;
+    pa.nreal = 1;
+    pa.stdu = w->stdu;
+    pa.seeds = d_seed;
+    pa.jumppoly = w->d_jump;
+    pa.upot = d_pot;
+    if ((rc = rg::launch_potential(pa, s))) return rc;
+    a.upot = d_pot;
+    a.pot_xstride = w->ny;
+    a.pot_ystride = 1;
   } else {
     // caller layout upot(nxdiso, ny), x fastest
     RG_CUDA(cudaMemcpyAsync(d_pot, h_upot, pot, cudaMemcpyHostToDevice, s));
     a.upot = d_pot;
-    a.pot_rstride = 0;
     a.pot_xstride = 1;
     a.pot_ystride = w->p.nxdiso;
   }
+  a.pot_rstride = 0;
   a.tout = (h_t || h_tfilt) ? d_t : nullptr;
   a.teig = d_teig;
   a.status = d_status;
   RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
   if ((rc = rg::launch_sweep(a, s, grid))) return rc;
-  int32_t st = 0;
-  RG_CUDA(cudaMemcpyAsync(&st, d_status, sizeof st, cudaMemcpyDeviceToHost, s));
+  if (want_r) {
+    rg::SweepArgs b = a;
+    b.mode = rg::kModeRefl;
+    b.tout = d_r;
+    b.status = d_status + 1;
+    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+    if ((rc = rg::launch_sweep(b, s, grid))) return rc;
+  }
+  int32_t st[2] = {0, 0};
+  RG_CUDA(cudaMemcpyAsync(st, d_status, sizeof(int32_t) * (want_r ? 2 : 1), cudaMemcpyDeviceToHost, s));
   if (h_teig) RG_CUDA(cudaMemcpyAsync(h_teig, d_teig, sizeof(double) * w->neigv, cudaMemcpyDeviceToHost, s));
   if (h_t) RG_CUDA(cudaMemcpyAsync(h_t, d_t, tbytes, cudaMemcpyDeviceToHost, s));
   if (h_tfilt) RG_CUDA(cudaMemcpyAsync(h_tfilt, d_t, tbytes, cudaMemcpyDeviceToHost, s));
+  if (h_r) RG_CUDA(cudaMemcpyAsync(h_r, d_r, rbytes, cudaMemcpyDeviceToHost, s));
   RG_CUDA(cudaStreamSynchronize(s));
-  if (st != RG_OK) return rg::fail(st, status_text(st));
+  const int bad = st[0] != RG_OK ? st[0] : st[1];
+  if (bad != RG_OK) return rg::fail(bad, status_text(bad));
   return RG_OK;
 }
 
@@ -654,15 +684,13 @@ int rg_tdistrib_upot(rg_waveguide* w, const double* upot, double* teigvals, doub
 
 int rg_compute_refl_trans_v1(rg_waveguide* w, int iseed, double* rmat, double* tmat) {
   if (!w || !tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v1: NULL argument");
-  if (rmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v1: r is not available yet (pass NULL)");
   const int32_t s = iseed;
-  return run_single(w, &s, nullptr, rg::kModeTmat, nullptr, tmat, nullptr);
+  return run_single(w, &s, nullptr, rg::kModeTmat, nullptr, tmat, nullptr, rmat);
 }
 
 int rg_refl_trans_v1_upot(rg_waveguide* w, const double* upot, double* rmat, double* tmat) {
   if (!w || !upot || !tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_upot: NULL argument");
-  if (rmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_upot: r is not available yet (pass NULL)");
-  return run_single(w, nullptr, upot, rg::kModeTmat, nullptr, tmat, nullptr);
+  return run_single(w, nullptr, upot, rg::kModeTmat, nullptr, tmat, nullptr, rmat);
 }
 
 int rg_potential(rg_waveguide* w, int iseed, double* upot) {

@@ -85,12 +85,26 @@ def test_compute_tdistrib_seed_and_chunks(pair):
     assert np.max(np.abs(tall[g.neigv: 2 * g.neigv] - ref)) <= TN_ABS
 
 
-def test_refl_trans_v1_t(pair):
+def test_refl_trans_v1(pair):
+    """t and r of compute_refl_trans_v1 (r from the reverse sweep) against the oracle's v1."""
     name, o, g = pair
     u = o.potential(4)
     ro, to = o.refl_trans_v1_upot(u)
-    tg = g.refl_trans_v1_upot(u)
-    assert relerr(tg, to) <= T_REL
+    rg_, tg = g.refl_trans_v1_upot(u, want_r=True)
+    assert relerr(tg, to) <= T_REL, name
+    assert relerr(rg_, ro) <= T_REL, name
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4, 5])
+def test_unitarity_on_gpu(seed):
+    """test_unitarity (src/waveguide.f90:561-590) with src/waveguide.test.f90:62-73: flux is
+    conserved at dabso = 0, ||t^H t + r^H r - 1|| ~ 0, through the seed-driven C ABI call."""
+    g = rg.Waveguide(**CASES["ref_test"])
+    assert g.test_unitarity(seed) < 1e-10
+    o = O.Waveguide(**CASES["ref_test"])
+    ro, to = o.refl_trans_v1_upot(o.potential(seed))
+    r, t = g.compute_refl_trans_v1(seed)
+    assert relerr(t, to) <= T_REL and relerr(r, ro) <= T_REL
 
 
 def test_batch_equals_single_and_oracle():
@@ -197,8 +211,11 @@ def test_large_refl_trans_v1_t():
     kw = LARGE["m72"]
     o, g = O.Waveguide(**kw), rg.Waveguide(**kw)
     u = o.potential(9)
-    _, to = o.refl_trans_v1_upot(u)
-    assert relerr(g.refl_trans_v1_upot(u), to) <= T_REL
+    ro, to = o.refl_trans_v1_upot(u)
+    rg_, tg = g.refl_trans_v1_upot(u, want_r=True)
+    assert relerr(tg, to) <= T_REL and relerr(rg_, ro) <= T_REL
+    d = tg.conj().T @ tg + rg_.conj().T @ rg_ - np.eye(g.nmu)
+    assert np.linalg.norm(d) < 1e-9  # dabso = 0: flux conservation (M=72, full matrices)
 
 
 def test_large_batch_matches_single():
