@@ -70,6 +70,8 @@ struct SweepArgs {
   int64_t work_stride;        // double2 elements per CTA
   int max_M, max_ny;          // largest M and ny among the items (shared-memory sizing)
   int cluster;                // CTAs per work item (large-mode kernel; set by sweep_plan)
+  int force_large;            // 1: use the blocked global-memory kernel even for max_M <= 64 (autotuner)
+  int force_cluster;          // > 0: cluster size for the blocked kernel instead of the heuristic (autotuner)
 };
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t

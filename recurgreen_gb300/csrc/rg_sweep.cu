@@ -548,6 +548,7 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
 }
 
 int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+  if (a.force_large) return sweep_large_plan(a, sm_count, grid, work_stride);
   if (a.max_M <= 16) return plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
   if (a.max_M <= 32) return plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
   if (a.max_M <= kMaxModesSmem) return plan_t<64, 256, 2>(a, sm_count, grid, work_stride);
@@ -556,6 +557,7 @@ int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
 
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
+  if (a.force_large) return launch_sweep_large(a, stream, grid);
   if (a.max_M <= 16) return launch_t<16, 64, 8>(a, stream, grid);
   if (a.max_M <= 32) return launch_t<32, 128, 4>(a, stream, grid);
   if (a.max_M <= kMaxModesSmem) return launch_t<64, 256, 2>(a, stream, grid);

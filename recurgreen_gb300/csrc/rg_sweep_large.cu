@@ -529,7 +529,11 @@ int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride
   if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "large-mode sweep kernel does not fit on an SM");
   const int slots = per_sm * sm_count;
   int C = 1;
-  while (C < kMaxCluster && (int64_t)a.nreal * C * 2 <= slots) C *= 2;
+  if (a.force_cluster > 0) {
+    while (C < kMaxCluster && C < a.force_cluster) C *= 2;
+  } else {
+    while (C < kMaxCluster && (int64_t)a.nreal * C * 2 <= slots) C *= 2;
+  }
   int nclusters = slots / C;
   if (C > 1) {
     cudaLaunchConfig_t cfg{};

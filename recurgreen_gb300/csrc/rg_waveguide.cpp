@@ -4,8 +4,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -193,6 +196,10 @@ struct rg_waveguide {
   size_t scratch_bytes = 0;
   cudaEvent_t ev_sweep0 = nullptr, ev_sweep1 = nullptr;  // around the last batch's sweep launches
   bool sweep_timed = false;
+  // The last batch launch, captured as a CUDA graph and replayed while its
+  // arguments (sizes, buffers, workspace, kernel choice) stay the same.
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_key[10] = {0};
 };
 
 namespace {
@@ -235,6 +242,8 @@ void free_device(rg_waveguide* w) {
   cudaFree(w->d_counter);
   cudaFree(w->d_desc);
   cudaFree(w->d_scratch);
+  if (w->graph) cudaGraphExecDestroy(w->graph);
+  w->graph = nullptr;
   if (w->ev_sweep0) cudaEventDestroy(w->ev_sweep0);
   if (w->ev_sweep1) cudaEventDestroy(w->ev_sweep1);
   w->ev_sweep0 = w->ev_sweep1 = nullptr;
@@ -448,21 +457,179 @@ int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
   return RG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner.  For a waveguide shape (M, ny) and a batch size, the candidate
+// launch configurations -- the shared-memory kernel or the blocked kernel
+// for M <= 64, and the blocked kernel's cluster size (CTAs per realization)
+// -- are timed once on a short proxy guide (the same modes and grid, 16
+// slices, the same number of realizations) and the fastest is cached for the
+// process.  RG_AUTOTUNE=0 disables it (the built-in heuristics decide).
+// ---------------------------------------------------------------------------
+struct TuneChoice {
+  int force_large = 0;
+  int force_cluster = 0;
+};
+
+struct TuneKey {
+  int M, ny, bucket, sms;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(M, ny, bucket, sms) < std::tie(o.M, o.ny, o.bucket, o.sms);
+  }
+};
+
+std::mutex g_tune_mutex;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+
+bool autotune_enabled() {
+  const char* e = std::getenv("RG_AUTOTUNE");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+
+int size_bucket(int n) {
+  int b = 1;
+  while (b < n && b < (1 << 20)) b <<= 1;
+  return b;
+}
+
+// Times one configuration on the proxy (ms); large values mean "unusable".
+double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const int32_t* d_seeds, double* d_teig,
+                      int32_t* d_status, const TuneChoice& tc, cudaStream_t s) {
+  rg::SweepArgs a = make_args(w, rg::kModeEig);
+  a.wgs = d_proxy;
+  a.nreal = n;
+  a.seeds = d_seeds;
+  a.teig = d_teig;
+  a.status = d_status;
+  a.force_large = tc.force_large;
+  a.force_cluster = tc.force_cluster;
+  int grid = 0;
+  int64_t stride = 0;
+  if (rg::sweep_plan(a, w->sm_count, &grid, &stride) != RG_OK) return 1e30;
+  const size_t need = sizeof(double2) * (size_t)stride * (grid / (a.cluster > 0 ? a.cluster : 1));
+  double2* ws = nullptr;
+  if (cudaMalloc((void**)&ws, need) != cudaSuccess) {
+    cudaGetLastError();
+    return 1e30;
+  }
+  a.work = ws;
+  a.work_stride = stride;
+  double best = 1e30;
+  for (int rep = 0; rep < 2; ++rep) {
+    cudaMemsetAsync(w->d_counter, 0, sizeof(int), s);
+    cudaEventRecord(w->ev_sweep0, s);
+    if (rg::launch_sweep(a, s, grid) != RG_OK) break;
+    cudaEventRecord(w->ev_sweep1, s);
+    float ms = 0.0f;
+    if (cudaEventSynchronize(w->ev_sweep1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, w->ev_sweep0, w->ev_sweep1) != cudaSuccess)
+      break;
+    if (rep > 0) best = ms;
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(ws);
+  cudaGetLastError();
+  return best;
+}
+
+TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
+  TuneChoice def;
+  if (!autotune_enabled() || n <= 0) return def;
+  const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return it->second;
+  }
+  std::vector<TuneChoice> cands;
+  if (w->nmu <= rg::kMaxModesSmem) {
+    cands.push_back(TuneChoice{0, 0});
+    if (w->nmu > 32) cands.push_back(TuneChoice{1, 1});
+  } else {
+    for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{1, c});
+  }
+  if (cands.size() == 1) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = cands[0];
+    return cands[0];
+  }
+  // Proxy: the same waveguide cut to 16 slices (all disordered).
+  rg::WgDesc pd = w->h_desc;
+  pd.nx = std::min(pd.nx, 16);
+  pd.nxfree = 0;
+  pd.nxdiso = pd.nx;
+  const int np = std::min(n, 4 * w->sm_count);
+  char* buf = nullptr;
+  const size_t b_desc = align256(sizeof pd), b_seed = align256(sizeof(int32_t) * np);
+  const size_t b_teig = align256(sizeof(double) * (size_t)np * w->neigv);
+  if (cudaMalloc((void**)&buf, b_desc + 2 * b_seed + b_teig) != cudaSuccess) {
+    cudaGetLastError();
+    return def;
+  }
+  rg::WgDesc* d_pd = (rg::WgDesc*)buf;
+  int32_t* d_seeds = (int32_t*)(buf + b_desc);
+  int32_t* d_status = (int32_t*)(buf + b_desc + b_seed);
+  double* d_teig = (double*)(buf + b_desc + 2 * b_seed);
+  std::vector<int32_t> seeds(np);
+  for (int k = 0; k < np; ++k) seeds[k] = k + 1;
+  cudaMemcpyAsync(d_pd, &pd, sizeof pd, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice, s);
+  TuneChoice best = cands[0];
+  double tbest = 1e30;
+  for (const TuneChoice& c : cands) {
+    const double t = time_candidate(w, d_pd, np, d_seeds, d_teig, d_status, c, s);
+    if (t < tbest) {
+      tbest = t;
+      best = c;
+    }
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(buf);
+  cudaGetLastError();
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_cache[key] = best;
+  return best;
+}
+
 // Seed-driven batch on device buffers: one persistent launch, the potential
 // of every item drawn inside the kernel.  d_seeds, d_teig, d_status are
 // device pointers.  CUDA events bracket the launch for rg_last_sweep_time.
+// The launch (counter reset and kernel) is captured as a CUDA graph the
+// first time a given argument set is seen and replayed afterwards.
 int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_teig, int32_t* d_status,
                    cudaStream_t s) {
+  const TuneChoice tc = autotune(w, n, s);
   rg::SweepArgs a = make_args(w, rg::kModeEig);
   a.nreal = n;
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
+  a.force_large = tc.force_large;
+  a.force_cluster = tc.force_cluster;
   int grid = 0, rc;
   if ((rc = place_workspace(w, a, 0, &grid))) return rc;
-  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  const int64_t key[10] = {n, (int64_t)(intptr_t)d_seeds, (int64_t)(intptr_t)d_teig, (int64_t)(intptr_t)d_status,
+                           (int64_t)(intptr_t)a.work, grid, a.cluster, a.force_large, a.work_stride, 1};
+  if (!w->graph || std::memcmp(key, w->graph_key, sizeof key) != 0) {
+    if (w->graph) cudaGraphExecDestroy(w->graph);
+    w->graph = nullptr;
+    cudaGraph_t gr = nullptr;
+    RG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(w->d_counter, 0, sizeof(int), s);
+    rc = (e == cudaSuccess) ? rg::launch_sweep(a, s, grid) : rg::cuda_fail(e, "graph capture");
+    const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+    if (rc) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    RG_CUDA(ec);
+    e = cudaGraphInstantiate(&w->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    RG_CUDA(e);
+    std::memcpy(w->graph_key, key, sizeof key);
+  }
+  // Timing events bracket the graph launch (events inside a graph cannot be timed).
   RG_CUDA(cudaEventRecord(w->ev_sweep0, s));
-  if ((rc = rg::launch_sweep(a, s, grid))) return rc;
+  RG_CUDA(cudaGraphLaunch(w->graph, s));
   RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
   w->sweep_timed = true;
   return RG_OK;

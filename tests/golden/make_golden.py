@@ -77,15 +77,16 @@ def main(ref: str) -> None:
     with open(os.path.join(HERE, "base_utils_kat.json"), "w") as f:
         json.dump(g, f, indent=1)
     samples = fortran_list_read(os.path.join(ref, "test", "test_data.csv"))
-    rows = []
+    rows, lines = [], []
     for line in open(os.path.join(ref, "test", "replot_1.distrib.csv")):
         if line.startswith("%") or line.startswith("tm") or not line.strip():
             continue
         a, b = line.split(",")
         rows.append([float(a), float(b)])
+        lines.append(line.rstrip("\n"))
     rep = {"source": "RecurGreen test/test_data.csv -> test/replot_1.distrib.csv (plothisto, chebyshev bins on [0, 1])",
            "bintype": "chebyshev", "xmin": 0.0, "xmax": 1.0, "nbins": len(rows),
-           "samples": [None if s != s else s for s in samples], "rho": rows}
+           "samples": [None if s != s else s for s in samples], "rho": rows, "lines": lines}
     with open(os.path.join(HERE, "replot_fixture.json"), "w") as f:
         json.dump(rep, f, indent=0)
 

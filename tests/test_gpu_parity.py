@@ -251,3 +251,49 @@ def test_multi_uneven_matches_single_and_oracle():
         o = O.Waveguide(**specs[k])
         g, s = items[k]
         assert np.max(np.abs(res[k] - o.tdistrib_upot(o.potential(s)))) <= TN_ABS
+
+
+def test_batch_graph_replay_and_autotune(monkeypatch):
+    """Repeated batch calls on the same device buffers replay a captured CUDA
+    graph; the autotuned kernel choice agrees with the heuristic choice."""
+    import ctypes
+
+    import torch
+
+    kw = CASES["m64"]
+    g = rg.Waveguide(**kw)
+    n = 20
+    seeds = torch.arange(1, n + 1, dtype=torch.int32, device="cuda")
+    out = torch.zeros(n * g.neigv, dtype=torch.float64, device="cuda")
+    st = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    L = rg.lib()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    vp = ctypes.c_void_p
+    res = []
+    for _ in range(3):  # capture, then two replays
+        out.zero_()
+        torch.cuda.synchronize()
+        rc = L.rg_tdistrib_batch_device(g._h, vp(seeds.data_ptr()), n, vp(out.data_ptr()), vp(st.data_ptr()),
+                                        vp(s.cuda_stream))
+        assert rc == 0, L.rg_last_error().decode()
+        res.append(out.cpu().numpy().copy())
+    assert np.all(st.cpu().numpy() == 0)
+    np.testing.assert_array_equal(res[0], res[1])
+    np.testing.assert_array_equal(res[0], res[2])
+    ms = ctypes.c_float()
+    assert L.rg_last_sweep_time(g._h, ctypes.byref(ms)) == 0 and ms.value > 0
+    monkeypatch.setenv("RG_AUTOTUNE", "0")
+    ref = rg.Waveguide(**kw).tdistrib_batch(np.arange(1, n + 1, dtype=np.int32))
+    assert np.max(np.abs(ref - res[0])) <= 1e-12
+
+
+def test_large_autotuned_cluster_matches():
+    kw = dict(LARGE["m128"], nxdiso=6)
+    g = rg.Waveguide(**kw)
+    seeds = np.arange(1, 9, dtype=np.int32)
+    b = g.tdistrib_batch(seeds)  # autotuned cluster size
+    for k, s in enumerate(seeds[:3]):
+        one = np.zeros(s * g.neigv)
+        g.compute_tdistrib(int(s), one)  # single realization: cluster of 8
+        assert np.max(np.abs(b[k * g.neigv:(k + 1) * g.neigv] - one[(s - 1) * g.neigv:])) <= 1e-12
