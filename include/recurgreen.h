@@ -90,6 +90,10 @@ int rg_get_parameters(const rg_waveguide* wg, rg_params* out);
  * deviation stdu of the dimensionless potential (src/waveguide.f90:118,243,370). */
 int rg_get_scalars(const rg_waveguide* wg, double* kdx, double* dos, double* stdu);
 
+/* The mode set's direction cosines mumesh and the diagonal of B
+ * (src/waveguide.f90:240-248), nmu complex values each (either may be NULL). */
+int rg_get_modes(const rg_waveguide* wg, double* mumesh, double* bmat);
+
 /* compute_tdistrib (src/waveguide.f90:392-462): draws the disorder of seed
  * `iseed`, runs the recursive Green sweep on the GPU, and writes the neigv
  * transmission eigenvalues (descending) into chunk iseed of the host array
@@ -140,6 +144,31 @@ int rg_tdistrib_batch_device(rg_waveguide* wg, const int32_t* d_seeds, int n, do
  * per-item status; the first non-OK status is returned after all items ran. */
 int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, const int64_t* offsets,
                       double* tallvals, int64_t len, int32_t* status);
+
+/* Adjoint support (no counterpart in the reference, whose FP64 path has no
+ * gradients).  Device pointers; work is enqueued on `stream` taken literally
+ * (0 is CUDA's default stream, as frameworks pass it), no synchronisation.
+ *
+ * rg_sweep_segment runs the recursion of n realizations over slices
+ * [n_begin, n_end) on caller-given potentials d_upot (n x nxdiso x ny,
+ * C order), starting from d_state_in (n x 2 x nmu x nmu complex, row-major:
+ * Gss then Gs1 after slice n_begin-1; NULL exactly when n_begin == 0).  It
+ * writes the state after every slice to d_state_dump (n x (n_end-n_begin) x
+ * 2 x nmu x nmu, optional) and after the last one to d_state_out (optional).
+ * When n_end == nx it also forms the filtered Fisher-Lee t (d_tfilt,
+ * n x ncol x nrow complex, i.e. column-major per realization, optional) and
+ * the eigenvalues (d_teig, n x neigv).  This is the forward recomputation
+ * from checkpoints of the adjoint sweep.
+ *
+ * rg_adjoint_grad_rows turns the adjoints Xbar = dL/dX* of n slice matrices
+ * (n x nmu x nmu complex, row-major) into the potential gradients
+ * dL/dU(n, :) = -2 sum Re(Xbar[a][c]) chi_a chi_c, n rows of ny doubles
+ * grad_stride apart (Dirichlet guides). */
+int rg_sweep_segment(rg_waveguide* wg, const double* d_upot, int n, int n_begin, int n_end,
+                     const double* d_state_in, double* d_state_dump, double* d_state_out, double* d_tfilt,
+                     double* d_teig, int32_t* d_status, void* stream);
+int rg_adjoint_grad_rows(rg_waveguide* wg, const double* d_xbar, int n, double* d_grad, int64_t grad_stride,
+                         void* stream);
 
 /* Tracing (the reference times its seed loop with date_and_time,
  * src/main.f90:145,174-176): device time in milliseconds of the sweep kernel

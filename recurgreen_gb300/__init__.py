@@ -26,7 +26,8 @@ EXPORTS = (
     "rg_get_ny", "rg_get_nprop", "rg_get_window", "rg_get_xmesh", "rg_get_parameters", "rg_get_scalars",
     "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
-    "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi",
+    "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi", "rg_sweep_segment",
+    "rg_adjoint_grad_rows", "rg_get_modes",
 )
 
 
@@ -75,6 +76,9 @@ def lib() -> C.CDLL:
     L.rg_tdistrib_seed_noalloc.argtypes = [vp, C.c_int, vp, vp, vp]
     L.rg_last_sweep_time.argtypes = [vp, C.POINTER(C.c_float)]
     L.rg_tdistrib_multi.argtypes = [C.POINTER(vp), ip, C.c_int, C.POINTER(C.c_int64), dp, i64, ip]
+    L.rg_sweep_segment.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp]
+    L.rg_adjoint_grad_rows.argtypes = [vp, vp, C.c_int, vp, i64, vp]
+    L.rg_get_modes.argtypes = [vp, vp, vp]
     _LIB = L
     return L
 
@@ -152,6 +156,13 @@ class Waveguide:
         x = np.zeros(self.nx, np.float64)
         _check(lib().rg_get_xmesh(self._h, _dp(x), x.size))
         return x
+
+    def get_modes(self):
+        """(mumesh, bmat): nmu complex values each (src/waveguide.f90:240-248)."""
+        mu = np.zeros(self.nmu, np.complex128)
+        b = np.zeros(self.nmu, np.complex128)
+        _check(lib().rg_get_modes(self._h, mu.ctypes.data, b.ctypes.data))
+        return mu, b
 
     def get_parameters(self) -> dict:
         p = rg_params()

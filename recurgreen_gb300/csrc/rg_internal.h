@@ -70,6 +70,12 @@ struct SweepArgs {
   int64_t work_stride;        // double2 elements per CTA
   int max_M, max_ny;          // largest M and ny among the items (shared-memory sizing)
   int cluster;                // CTAs per work item (large-mode kernel; set by sweep_plan)
+  // Segment mode (blocked kernel only; used by the adjoint's recomputation):
+  // run slices [n_begin, n_end) from a given state and dump the states.
+  int n_begin, n_end;         // slice range; n_end == 0 means the whole guide
+  const double2* state_in;    // [nreal][2][M][M] (Gss, Gs1) after slice n_begin-1, natural order; nullptr: fresh start
+  double2* state_dump;        // [nreal][n_end-n_begin][2][M][M] (Gss, Gs1) after every slice, optional
+  double2* state_out;         // [nreal][2][M][M] state after slice n_end-1, optional
   int force_large;            // 1: use the blocked global-memory kernel even for max_M <= 64 (autotuner)
   int force_cluster;          // > 0: cluster size for the blocked kernel instead of the heuristic (autotuner)
 };
@@ -97,6 +103,9 @@ int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid);
 // The large-mode kernel behind sweep_plan/launch_sweep for max_M > kMaxModesSmem (rg_sweep_large.cu).
 int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
+// Adjoint (rg_adjoint.cu): dL/dU rows of n realizations from their slice-matrix adjoints.
+int launch_grad_rows(const WgDesc* d_desc, int M, const double2* xbar, int n, double* grad, int64_t gstride,
+                     cudaStream_t s);
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,
                      unsigned long long* d_counts, cudaStream_t stream);
 

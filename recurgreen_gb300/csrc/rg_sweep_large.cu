@@ -115,7 +115,23 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       sinv[c] = c;
       used[c] = 0;
     }
-    for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    const int nb = a.n_begin, ne = a.n_end > 0 ? a.n_end : wd.nx;
+    if (a.state_in) {
+      // Resume after slice nb-1 from a natural-order state: Gss goes to the
+      // buffer the first slice reads, R holds Y with Gs1 = rsign * Y.
+      const double2* sin = a.state_in + (int64_t)r * 2 * mm;
+      const double rs = (nb == 1) ? 1.0 : -1.0;
+      for (int64_t e = ctid; e < mm; e += CNT) {
+        Wb0[e] = sin[e];
+        Rg[e] = cscale(rs, sin[mm + e]);
+      }
+      for (int c = tid; c < M; c += NT) {
+        pinv[c] = c;
+        colmap[c] = c;
+      }
+    } else {
+      for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    }
     if (draw) {
       for (int iy = ctid; iy < ny; iy += CNT) {
         const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
@@ -129,7 +145,7 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
     cluster.sync();
 
     int cur = 0;
-    for (int n = 0; n < wd.nx; ++n) {
+    for (int n = nb; n < ne; ++n) {
       const int id = (refl ? wd.nx - 1 - n : n) - wd.nxfree;  // slice of the guide swept at step n
       const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
@@ -386,6 +402,36 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         used[c] = 0;
       }
       __syncthreads();
+      // Segment mode: the natural-order state after this slice,
+      // Gss[a][c] = W[piv[a]][colmap[c]] and Gs1[a][j] = sign * R[piv[a]][j].
+      const bool last = (n == ne - 1);
+      if (a.state_dump || (a.state_out && last)) {
+        const double2* Wn = cur ? Wb1 : Wb0;
+        const double gs = (n == 0) ? 1.0 : -1.0;
+        double2* d1 = a.state_dump ? a.state_dump + ((int64_t)r * (ne - nb) + (n - nb)) * 2 * mm : nullptr;
+        double2* d2 = (a.state_out && last) ? a.state_out + (int64_t)r * 2 * mm : nullptr;
+        for (int64_t e = ctid; e < mm; e += CNT) {
+          const int ar = (int)(e / M), c = (int)(e % M);
+          const double2 gss = __ldcg(Wn + (int64_t)piv[ar] * M + colmap[c]);
+          const double2 gs1 = cscale(gs, __ldcg(Rg + (int64_t)piv[ar] * M + c));
+          if (d1) {
+            d1[e] = gss;
+            d1[mm + e] = gs1;
+          }
+          if (d2) {
+            d2[e] = gss;
+            d2[mm + e] = gs1;
+          }
+        }
+        cluster.sync();  // R is rescaled in place by the next slice
+      }
+    }
+
+    if (ne < wd.nx) {  // a partial sweep (segment): no Fisher-Lee stage
+      __syncthreads();
+      if (rank == 0 && tid == 0) a.status[r] = s_status;
+      cluster.sync();
+      continue;
     }
 
     if (refl) {

@@ -827,6 +827,13 @@ int rg_get_scalars(const rg_waveguide* w, double* kdx, double* dos, double* stdu
   return RG_OK;
 }
 
+int rg_get_modes(const rg_waveguide* w, double* mumesh, double* bmat) {
+  if (!w) return rg::fail(RG_ERR_INVALID_ARG, "rg_get_modes: NULL handle");
+  if (mumesh) std::memcpy(mumesh, w->mumesh.data(), sizeof(cplx) * w->nmu);
+  if (bmat) std::memcpy(bmat, w->bmat.data(), sizeof(cplx) * w->nmu);
+  return RG_OK;
+}
+
 int rg_compute_tdistrib(rg_waveguide* w, int iseed, double* tallvals, int64_t len) {
   if (!w || !tallvals) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_tdistrib: NULL argument");
   // Chunk checks of src/waveguide.f90:408-421.
@@ -1051,6 +1058,50 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
   }
   if (bad) return rg::fail(bad, status_text(bad));
   return RG_OK;
+}
+
+int rg_sweep_segment(rg_waveguide* w, const double* d_upot, int n, int n_begin, int n_end, const double* d_state_in,
+                     double* d_state_dump, double* d_state_out, double* d_tfilt, double* d_teig, int32_t* d_status,
+                     void* stream) {
+  if (!w || !d_upot || !d_status || n < 0) return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: invalid argument");
+  if (n_begin < 0 || n_end <= n_begin || n_end > w->nx)
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: need 0 <= n_begin < n_end <= nx");
+  if ((n_begin > 0) != (d_state_in != nullptr))
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: a state is given exactly when n_begin > 0");
+  if (n_end == w->nx && !d_teig) return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: the last segment needs d_teig");
+  if (n == 0) return RG_OK;
+  DeviceGuard g(w->device);
+  cudaStream_t s = (cudaStream_t)stream;  // taken literally: 0 is CUDA's default stream
+  rg::SweepArgs a = make_args(w, rg::kModeEig);
+  a.nreal = n;
+  a.force_large = 1;
+  a.upot = d_upot;
+  a.pot_rstride = (int64_t)w->p.nxdiso * w->ny;
+  a.pot_xstride = w->ny;
+  a.pot_ystride = 1;
+  a.n_begin = n_begin;
+  a.n_end = n_end;
+  a.state_in = (const double2*)d_state_in;
+  a.state_dump = (double2*)d_state_dump;
+  a.state_out = (double2*)d_state_out;
+  a.tout = (double2*)d_tfilt;
+  a.teig = d_teig;
+  a.status = d_status;
+  int grid = 0, rc;
+  if ((rc = place_workspace(w, a, 0, &grid))) return rc;
+  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  return rg::launch_sweep(a, s, grid);
+}
+
+int rg_adjoint_grad_rows(rg_waveguide* w, const double* d_xbar, int n, double* d_grad, int64_t grad_stride,
+                         void* stream) {
+  if (!w || !d_xbar || !d_grad || n < 0) return rg::fail(RG_ERR_INVALID_ARG, "rg_adjoint_grad_rows: invalid argument");
+  if (w->p.boundtype != RG_BOUND_DIRICHLET)
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_adjoint_grad_rows: the adjoint supports Dirichlet guides only");
+  if (grad_stride < w->ny) return rg::fail(RG_ERR_INVALID_ARG, "rg_adjoint_grad_rows: grad_stride < ny");
+  DeviceGuard g(w->device);
+  cudaStream_t s = (cudaStream_t)stream;  // taken literally: 0 is CUDA's default stream
+  return rg::launch_grad_rows(w->d_desc, w->nmu, (const double2*)d_xbar, n, d_grad, grad_stride, s);
 }
 
 int rg_last_sweep_time(rg_waveguide* w, float* ms) {

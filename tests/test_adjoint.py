@@ -1,0 +1,97 @@
+"""The hand-written adjoint sweep behind torch.autograd, checked against
+central finite differences of the CPU oracle (step 1e-6 * sigma_U), with the
+bar |dL/dU adjoint - FD| <= 1e-6 relative to the largest sampled gradient."""
+import numpy as np
+import pytest
+
+import oracle as O
+import recurgreen_gb300 as rg
+
+pytestmark = pytest.mark.gpu
+
+FD_REL = 1e-6
+
+
+def _losses_oracle(o, u):
+    _, t = o.tdistrib_upot(u, want_t=True)
+    A = t.conj().T @ t
+    return float(np.sum(np.abs(t) ** 2)), float(np.sum(np.abs(A) ** 2))
+
+
+def _check(kw, B, K, ncell, seed0):
+    torch = pytest.importorskip("torch")
+    from recurgreen_gb300.adjoint import transmission_losses
+
+    o, g = O.Waveguide(**kw), rg.Waveguide(**kw)
+    us = [o.potential(seed0 + r) for r in range(B)]  # (ny, nxdiso) each
+    U = torch.tensor(np.stack([u.T for u in us]), dtype=torch.float64, device="cuda", requires_grad=True)
+    L1, L2 = transmission_losses(U, g, K)
+    for r in range(B):  # forward parity: the segmented sweep gives the oracle's losses
+        l1, l2 = _losses_oracle(o, us[r])
+        assert abs(L1[r].item() - l1) <= 1e-10 * abs(l1) and abs(L2[r].item() - l2) <= 1e-10 * abs(l2)
+    rng = np.random.default_rng(seed0)
+    h = 1e-6 * o.stdu
+    for which, L in (("L1", L1), ("L2", L2)):
+        (gU,) = torch.autograd.grad(L.sum(), U, retain_graph=True)
+        gU = gU.cpu().numpy()
+        for r in range(B):
+            cells = [(int(rng.integers(0, o.nxdiso)), int(rng.integers(0, o.ny))) for _ in range(ncell)]
+            fd = []
+            for ix, iy in cells:
+                up, um = us[r].copy(), us[r].copy()
+                up[iy, ix] += h
+                um[iy, ix] -= h
+                k = 0 if which == "L1" else 1
+                fd.append((_losses_oracle(o, up)[k] - _losses_oracle(o, um)[k]) / (2 * h))
+            fd = np.array(fd)
+            adj = np.array([gU[r, ix, iy] for ix, iy in cells])
+            scale = np.max(np.abs(fd))
+            assert np.max(np.abs(adj - fd)) <= FD_REL * scale, (which, r, np.max(np.abs(adj - fd)) / scale)
+
+
+def test_adjoint_small_absorbing():
+    kw = dict(boundtype="dirichlet", nxdiso=14, nxfree=1, wol=6.25, exfac=1.0, aratio=1.0, dscat=3.0, dabso=0.3,
+              ny=24)
+    _check(kw, B=2, K=4, ncell=10, seed0=3)
+
+
+def test_adjoint_differentiation_width():
+    """The differentiation config's modes and grid (M=128, ny=512), a short guide."""
+    kw = dict(boundtype="dirichlet", nxdiso=24, nxfree=0, wol=64.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=512)
+    _check(kw, B=1, K=5, ncell=6, seed0=11)
+
+
+def test_segmented_forward_matches_one_sweep():
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    kw = dict(boundtype="dirichlet", nxdiso=30, nxfree=2, wol=10.25, exfac=1.0, aratio=1.0, dscat=4.0, ny=40)
+    g = rg.Waveguide(**kw)
+    o = O.Waveguide(**kw)
+    u = o.potential(2)
+    T1, t1 = g.tdistrib_upot(u, want_t=True)
+    U = torch.tensor(u.T[None].copy(), dtype=torch.float64, device="cuda")
+    M = g.nmu
+    L = rg.lib()
+    vp = ctypes.c_void_p
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s1 = torch.empty(1, 2, M, M, dtype=torch.complex128, device="cuda")
+    dump = torch.empty(1, g.nx - 13, 2, M, M, dtype=torch.complex128, device="cuda")
+    tf = torch.empty(1, g.jmax - g.jmin + 1, g.imax - g.imin + 1, dtype=torch.complex128, device="cuda")
+    te = torch.empty(1, g.neigv, dtype=torch.float64, device="cuda")
+    cs = vp(torch.cuda.current_stream().cuda_stream)
+    assert L.rg_sweep_segment(g._h, vp(U.data_ptr()), 1, 0, 13, None, None, vp(s1.data_ptr()), None, None,
+                              vp(st.data_ptr()), cs) == 0
+    assert L.rg_sweep_segment(g._h, vp(U.data_ptr()), 1, 13, g.nx, vp(s1.data_ptr()), vp(dump.data_ptr()), None,
+                              vp(tf.data_ptr()), vp(te.data_ptr()), vp(st.data_ptr()), cs) == 0
+    torch.cuda.synchronize()
+    assert st.item() == 0
+    t = tf[0].T.cpu().numpy()
+    assert np.linalg.norm(t - t1) / np.linalg.norm(t1) <= 1e-12
+    assert np.max(np.abs(te[0].cpu().numpy() - T1)) <= 1e-12
+    # the last dumped state is the final slice's: t = 2i S Gs1 S
+    mu, _ = g.get_modes()
+    sq = np.sqrt(mu)
+    gs1 = dump[0, -1, 1].cpu().numpy()
+    tt = 2j * sq[:, None] * gs1 * sq[None, :]
+    assert np.linalg.norm(tt - t1) / np.linalg.norm(t1) <= 1e-12
