@@ -171,11 +171,28 @@ int rg_adjoint_grad_rows(rg_waveguide* wg, const double* d_xbar, int n, double* 
                          void* stream);
 
 /* Tracing (the reference times its seed loop with date_and_time,
- * src/main.f90:145,174-176): device time in milliseconds of the sweep kernel
- * launched by the last rg_tdistrib_batch[_device] call on this handle,
- * measured with CUDA events recorded around that launch on its stream.
- * Fails if the last batch needed more than one sweep launch. */
+ * src/main.f90:145,174-176): device time in milliseconds of the sweep
+ * launches of the last rg_tdistrib_batch[_device] call on this handle (one
+ * kernel, or the symmetric kernel and its pivoted re-run), measured with CUDA
+ * events recorded around them on their stream.  Fails before the first batch. */
 int rg_last_sweep_time(rg_waveguide* wg, float* ms);
+
+/* No counterpart in the reference.  The launch configuration of the last
+ * rg_tdistrib_batch[_device] call on this handle: the sweep kernel that ran,
+ * its grid, and how many realizations the symmetric kernel handed to the
+ * pivoted kernel (their diagonal pivots fell below the threshold).  Waits for
+ * that batch to finish.  rerun is valid until the next computation on the
+ * handle. */
+#define RG_KERNEL_PIVOTED 0   /* shared-memory Gauss-Jordan with implicit partial pivoting */
+#define RG_KERNEL_SYMMETRIC 1 /* symmetric sweep (Dirichlet), pivoted re-run of flagged items */
+#define RG_KERNEL_BLOCKED 2   /* blocked global-memory kernel, `cluster` CTAs per realization */
+typedef struct rg_batch_info {
+  int kernel;  /* RG_KERNEL_* */
+  int grid;    /* CTAs of the launch */
+  int cluster; /* CTAs per realization */
+  int rerun;   /* realizations re-run by the pivoted kernel */
+} rg_batch_info;
+int rg_last_batch_info(rg_waveguide* wg, rg_batch_info* info);
 
 /* No counterpart in the reference.  One seed's transmission eigenvalues, as
  * rg_compute_tdistrib computes them, for callers that cannot allocate device

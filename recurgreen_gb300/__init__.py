@@ -27,8 +27,9 @@ EXPORTS = (
     "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
     "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi", "rg_sweep_segment",
-    "rg_adjoint_grad_rows", "rg_get_modes",
+    "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info",
 )
+KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked"}
 
 
 class RecurGreenError(RuntimeError):
@@ -37,6 +38,10 @@ class RecurGreenError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"[status {code}] {msg}")
         self.code = code
+
+
+class rg_batch_info(C.Structure):
+    _fields_ = [("kernel", C.c_int), ("grid", C.c_int), ("cluster", C.c_int), ("rerun", C.c_int)]
 
 
 class rg_params(C.Structure):
@@ -79,6 +84,7 @@ def lib() -> C.CDLL:
     L.rg_sweep_segment.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp]
     L.rg_adjoint_grad_rows.argtypes = [vp, vp, C.c_int, vp, i64, vp]
     L.rg_get_modes.argtypes = [vp, vp, vp]
+    L.rg_last_batch_info.argtypes = [vp, C.POINTER(rg_batch_info)]
     _LIB = L
     return L
 
@@ -229,6 +235,14 @@ class Waveguide:
             return out, st
         _check(rc)
         return out
+
+
+    def last_batch_info(self) -> dict:
+        """Kernel, grid, cluster and pivoted re-runs of the last tdistrib_batch."""
+        info = rg_batch_info()
+        _check(lib().rg_last_batch_info(self._h, C.byref(info)))
+        return {"kernel": KERNELS.get(info.kernel, str(info.kernel)), "grid": info.grid, "cluster": info.cluster,
+                "rerun": info.rerun}
 
 
 def tdistrib_multi(items, return_status: bool = False):

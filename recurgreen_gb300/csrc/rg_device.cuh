@@ -92,4 +92,97 @@ __device__ __forceinline__ double scaled_normal(double stdu, Xoshiro& st) {
   return stdu * (sqrt(-2.0 * log(u1)) * cos(twopi * u2));
 }
 
+// Eigenvalues of t^H t for the nrow x ncol matrix t held in shared memory at
+// W[i * LDW + j], by one-sided (Hestenes) Jacobi on the vectors of the smaller
+// dimension: columns of t if nrow >= ncol, else rows (the singular values of
+// t^T equal those of t).  The largest neigv of T_k = |v_k|^2 go to out in
+// descending order.  Every thread of the NT-thread block calls this; cc
+// (min(nrow, ncol) doubles) and *rot are shared scratch.  Returns false when
+// 60 sweeps did not converge (the same value in every thread).
+template <int NT>
+__device__ bool tt_eigenvalues(double2* W, int LDW, int nrow, int ncol, int neigv, double* cc, int* rot,
+                               double* out) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool bycol = nrow >= ncol;
+  const int nv = bycol ? ncol : nrow;
+  const int L = bycol ? nrow : ncol;
+  const int es = bycol ? LDW : 1;  // element stride inside a vector
+  const int vs = bycol ? 1 : LDW;  // stride between vectors
+  const int NP = (nv + 1) & ~1;
+  const double tol = 2.220446049250313e-16 * L;
+  int sweep = 0;
+  for (; sweep < 60; ++sweep) {
+    if (threadIdx.x == 0) *rot = 0;
+    __syncthreads();
+    for (int rr = 0; rr < NP - 1; ++rr) {
+      // round-robin pairing: position 0 fixed, the others rotate
+      for (int pk = warp; pk < NP / 2; pk += NW) {
+        const int pos1 = pk, pos2 = NP - 1 - pk;
+        const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
+        const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
+        if (vp >= nv || vq >= nv) continue;
+        double2* xp = W + vp * vs;
+        double2* xq = W + vq * vs;
+        double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+        for (int i = lane; i < L; i += 32) {
+          const double2 u = xp[i * es], w = xq[i * es];
+          al = fma(u.x, u.x, fma(u.y, u.y, al));
+          be = fma(w.x, w.x, fma(w.y, w.y, be));
+          gr = fma(u.x, w.x, fma(u.y, w.y, gr));   // re(conj(u) w)
+          gi = fma(u.x, w.y, fma(-u.y, w.x, gi));  // im(conj(u) w)
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, off);
+          be += __shfl_xor_sync(0xffffffffu, be, off);
+          gr += __shfl_xor_sync(0xffffffffu, gr, off);
+          gi += __shfl_xor_sync(0xffffffffu, gi, off);
+        }
+        const double ga = sqrt(gr * gr + gi * gi);
+        if (ga > tol * sqrt(al * be) && ga > 1e-300) {
+          if (lane == 0) *rot = 1;
+          const double zeta = (be - al) / (2.0 * ga);
+          const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
+                                              : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+          const double2 ph = make_double2(gr / ga, -gi / ga);  // exp(-i phi), gamma = |gamma| exp(i phi)
+          for (int i = lane; i < L; i += 32) {
+            const double2 u = xp[i * es];
+            const double2 w = cmul(ph, xq[i * es]);
+            xp[i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
+            xq[i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (!*rot) break;
+    __syncthreads();
+  }
+  // T_k = |v_k|^2, ranked in descending order (ties by index).
+  for (int k = warp; k < nv; k += NW) {
+    const double2* xk = W + k * vs;
+    double s = 0.0;
+    for (int i = lane; i < L; i += 32) {
+      const double2 u = xk[i * es];
+      s = fma(u.x, u.x, fma(u.y, u.y, s));
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) cc[k] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nv; k += NT) {
+    const double tk = cc[k];
+    int rank = 0;
+    for (int j = 0; j < nv; ++j) {
+      const double tj = cc[j];
+      rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+    }
+    if (rank < neigv) out[rank] = tk;
+  }
+  return sweep < 60;
+}
+
 }  // namespace rg

@@ -65,7 +65,8 @@ struct SweepArgs {
   double* teig;               // eigenvalues (kModeEig)
   double2* tout;              // [nreal][nrow * ncol] column-major t, optional (items of one waveguide only)
   int32_t* status;            // [nreal]
-  int* work_counter;          // persistent-scheduling counter, zeroed before launch
+  int* work_counter;          // kQueueCounters ints, zeroed before launch: [0] the work queue,
+                              // [1] items flagged by the symmetric kernel, [2] their re-run queue
   double2* work;              // per-CTA workspace in global memory
   int64_t work_stride;        // double2 elements per CTA
   int max_M, max_ny;          // largest M and ny among the items (shared-memory sizing)
@@ -77,8 +78,25 @@ struct SweepArgs {
   double2* state_dump;        // [nreal][n_end-n_begin][2][M][M] (Gss, Gs1) after every slice, optional
   double2* state_out;         // [nreal][2][M][M] state after slice n_end-1, optional
   int force_large;            // 1: use the blocked global-memory kernel even for max_M <= 64 (autotuner)
+  // Symmetric sweep (Dirichlet items, max_M <= kMaxModesSmem): the symmetric
+  // kernel runs every item and appends those it cannot pivot stably to
+  // flag_list; the pivoted kernel then re-runs that list.
+  int symmetric;              // 1: symmetric kernel first (needs flag_list)
+  int32_t* flag_list;         // [nreal] flagged item indices
+  double sym_tau;             // smallest accepted |diagonal pivot| / max |unswept entry of its row|
+  // Queue indirection of the pivoted kernel (set by launch_sweep for the re-run):
+  const int32_t* item_idx;    // [count] item index of queue position q; nullptr: q itself
+  const int* count_ptr;       // device-side queue length; nullptr: nreal
   int force_cluster;          // > 0: cluster size for the blocked kernel instead of the heuristic (autotuner)
 };
+
+// Status the symmetric kernel leaves on an item whose diagonal pivots were
+// too small; the pivoted kernel recomputes such items (never returned).
+constexpr int kStatusNeedPivot = 64;
+// Queue counters behind SweepArgs::work_counter.
+constexpr int kQueueCounters = 3;
+// Default of SweepArgs::sym_tau.
+constexpr double kSymTau = 0.1;
 
 constexpr int kModeEig = 0;   // tdistrib: filtered t -> eigenvalues of t^H t
 constexpr int kModeTmat = 1;  // v1 t: full t written to tout
@@ -100,6 +118,11 @@ struct PotArgs {
 int launch_potential(const PotArgs& a, cudaStream_t stream);
 int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid);
+// Symmetric sweep (rg_sweep_sym.cu): complex-symmetric slice matrices
+// (Dirichlet), M <= kMaxModesSmem, diagonal pivoting.  launch_sweep calls it
+// when a.symmetric is set and re-runs the flagged items itself.
+int sweep_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int launch_sweep_sym(const SweepArgs& a, cudaStream_t stream, int grid);
 // The large-mode kernel behind sweep_plan/launch_sweep for max_M > kMaxModesSmem (rg_sweep_large.cu).
 int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
@@ -120,6 +143,8 @@ struct NoAllocView {
   const uint64_t* jumppoly;
   cudaStream_t stream;
   const WgDesc* d_desc;
+  int symmetric;   // SweepArgs::symmetric for this guide
+  double sym_tau;  // SweepArgs::sym_tau
 };
 int noalloc_view(const rg_waveguide* w, NoAllocView* out);
 

@@ -11,7 +11,8 @@
 // already exists.
 //
 // The per-call scratch (the disorder potential of the realization, the seed,
-// the work-queue counter and, above 64 modes, the elimination matrices) lives
+// the work-queue counters, the symmetric sweep's flag slot and, above 64
+// modes, the elimination matrices) lives
 // in a file-scope __device__ array of fixed size, kNoAllocScratchBytes =
 // 16 MiB.  Every GPU that loads this library
 // holds that array until the process exits.  Its device address is looked up
@@ -28,15 +29,16 @@
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
-constexpr size_t kNoAllocHeaderBytes = 256;         // seed, counter
+constexpr size_t kNoAllocHeaderBytes = 256;         // seed, queue counters, flag slot
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Writes the seed and zeroes the work counter in the header of the array.
+// Writes the seed and zeroes the queue counters in the header of the array:
+// int32 [0] seed, [1, 1 + kQueueCounters) counters, then the flag slot.
 __global__ void noalloc_header_kernel(int32_t seed) {
   int32_t* hdr = reinterpret_cast<int32_t*>(g_noalloc_scratch);
   hdr[0] = seed;  // seed read by the potential generator
-  hdr[1] = 0;     // work-queue counter of the sweep
+  for (int k = 1; k <= rg::kQueueCounters; ++k) hdr[k] = 0;
 }
 
 constexpr int kMaxDevices = 64;
@@ -76,6 +78,8 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   a.max_ny = v.ny;
   a.teig = d_teigvals;
   a.status = d_status;
+  a.symmetric = v.symmetric;
+  a.sym_tau = v.sym_tau;
   int grid = 1;
   int64_t stride = 0;
   if ((rc = rg::sweep_plan(a, v.sm_count, &grid, &stride))) return rc;
@@ -98,6 +102,7 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   if ((rc = noalloc_scratch_address(cur, &base))) return rc;
   int32_t* d_seed = reinterpret_cast<int32_t*>(base);
   int* d_counter = reinterpret_cast<int*>(base) + 1;
+  int32_t* d_flag = reinterpret_cast<int32_t*>(base) + 1 + rg::kQueueCounters;
   double* d_pot = reinterpret_cast<double*>(base + kNoAllocHeaderBytes);
   cudaStream_t s = stream ? (cudaStream_t)stream : v.stream;
 
@@ -118,6 +123,7 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
   a.pot_xstride = v.ny;
   a.pot_ystride = 1;
   a.work_counter = d_counter;
+  a.flag_list = a.symmetric ? d_flag : nullptr;
   a.work = large ? reinterpret_cast<double2*>(base + kNoAllocHeaderBytes + pot_bytes) : nullptr;
   a.work_stride = large ? stride : 0;
   return rg::launch_sweep(a, s, grid);

@@ -20,6 +20,8 @@
 // whole chip) is the roofline of the sweep; shared memory, registers and HBM
 // have ample headroom, so the kernel keeps each slice matrix resident in
 // shared memory and spends its FP64 operations only on the elimination.
+#include <algorithm>
+
 #include "rg_device.cuh"
 
 namespace rg {
@@ -114,12 +116,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
 
   for (;;) {
     if (tid == 0) {
-      s_r = atomicAdd(a.work_counter, 1);
-      if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
+      const int q = atomicAdd(a.work_counter, 1);
+      const int nq = a.count_ptr ? *a.count_ptr : a.nreal;
+      s_r = q < nq ? (a.item_idx ? a.item_idx[q] : q) : -1;
+      if (s_r >= 0) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
     }
     __syncthreads();
-    const int r = s_r;
-    if (r >= a.nreal) break;
+    const int r = s_r;  // item index (queue position mapped through item_idx)
+    if (r < 0) break;
     const int M = wd.M, ny = wd.ny, nx = wd.nx;
     if (tid == 0) s_status = RG_OK;
     for (int c = tid; c < M; c += NT) {
@@ -397,88 +401,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(SweepArgs a) {
         if (e < nrow * ncol) W[(e % nrow) * LDW + e / nrow] = tv[s];
       }
       __syncthreads();
-      // 6. Eigenvalues of t^H t by one-sided (Hestenes) Jacobi on the
-      //    vectors of the smaller dimension: columns of t if nrow >= ncol,
-      //    else rows (the singular values of t^T equal those of t).
-      const bool bycol = nrow >= ncol;
-      const int nv = bycol ? ncol : nrow;
-      const int L = bycol ? nrow : ncol;
-      const int es = bycol ? LDW : 1;  // element stride inside a vector
-      const int vs = bycol ? 1 : LDW;  // stride between vectors
-      const int NP = (nv + 1) & ~1;
-      const double tol = 2.220446049250313e-16 * L;
-      int sweep = 0;
-      for (; sweep < 60; ++sweep) {
-        if (tid == 0) s_rot = 0;
-        __syncthreads();
-        for (int rr = 0; rr < NP - 1; ++rr) {
-          for (int pk = warp; pk < NP / 2; pk += NW) {
-            const int pos1 = pk, pos2 = NP - 1 - pk;
-            const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
-            const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
-            if (vp >= nv || vq >= nv) continue;
-            double2* xp = W + vp * vs;
-            double2* xq = W + vq * vs;
-            double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
-            for (int i = lane; i < L; i += 32) {
-              const double2 u = xp[i * es], w = xq[i * es];
-              al = fma(u.x, u.x, fma(u.y, u.y, al));
-              be = fma(w.x, w.x, fma(w.y, w.y, be));
-              gr = fma(u.x, w.x, fma(u.y, w.y, gr));   // re(conj(u) w)
-              gi = fma(u.x, w.y, fma(-u.y, w.x, gi));  // im(conj(u) w)
-            }
-#pragma unroll
-            for (int off = 16; off; off >>= 1) {
-              al += __shfl_xor_sync(0xffffffffu, al, off);
-              be += __shfl_xor_sync(0xffffffffu, be, off);
-              gr += __shfl_xor_sync(0xffffffffu, gr, off);
-              gi += __shfl_xor_sync(0xffffffffu, gi, off);
-            }
-            const double ga = sqrt(gr * gr + gi * gi);
-            if (ga > tol * sqrt(al * be) && ga > 1e-300) {
-              if (lane == 0) s_rot = 1;
-              const double zeta = (be - al) / (2.0 * ga);
-              const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
-                                                  : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-              const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-              const double2 ph = make_double2(gr / ga, -gi / ga);  // exp(-i phi), gamma = |gamma| exp(i phi)
-              for (int i = lane; i < L; i += 32) {
-                const double2 u = xp[i * es];
-                const double2 w = cmul(ph, xq[i * es]);
-                xp[i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
-                xq[i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
-              }
-            }
-          }
-          __syncthreads();
-        }
-        if (!s_rot) break;
-        __syncthreads();
-      }
-      if (sweep == 60 && tid == 0) s_status = RG_ERR_NOCONV;
-      // T_k = |v_k|^2, sorted descending into teig.
-      for (int k = warp; k < nv; k += NW) {
-        const double2* xk = W + k * vs;
-        double s = 0.0;
-        for (int i = lane; i < L; i += 32) {
-          const double2 u = xk[i * es];
-          s = fma(u.x, u.x, fma(u.y, u.y, s));
-        }
-#pragma unroll
-        for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (lane == 0) cc[k] = s;
-      }
-      __syncthreads();
+      // 6. Eigenvalues of t^H t, sorted descending into teig.
       const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
-      for (int k = tid; k < nv; k += NT) {
-        const double tk = cc[k];
-        int rank = 0;
-        for (int j = 0; j < nv; ++j) {
-          const double tj = cc[j];
-          rank += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
-        }
-        if (rank < wd.neigv) a.teig[obase + rank] = tk;
-      }
+      if (!tt_eigenvalues<NT>(W, LDW, nrow, ncol, wd.neigv, cc, &s_rot, a.teig + obase) && tid == 0)
+        s_status = RG_ERR_NOCONV;
     }
     __syncthreads();
     if (tid == 0) a.status[r] = s_status;
@@ -547,21 +473,51 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
   return RG_OK;
 }
 
+// Kernel choice: the blocked kernel when forced or above kMaxModesSmem
+// modes; otherwise the pivoted shared-memory kernel, preceded by the
+// symmetric kernel when a.symmetric is set.  Both shared-memory kernels then
+// run on the same grid and per-CTA workspace (the larger of their plans).
 int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
-  if (a.force_large) return sweep_large_plan(a, sm_count, grid, work_stride);
-  if (a.max_M <= 16) return plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
-  if (a.max_M <= 32) return plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
-  if (a.max_M <= kMaxModesSmem) return plan_t<64, 256, 2>(a, sm_count, grid, work_stride);
-  return sweep_large_plan(a, sm_count, grid, work_stride);
+  if (a.force_large || a.max_M > kMaxModesSmem) {
+    a.symmetric = 0;
+    return sweep_large_plan(a, sm_count, grid, work_stride);
+  }
+  int rc;
+  if (a.max_M <= 16) rc = plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
+  else if (a.max_M <= 32) rc = plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
+  else rc = plan_t<64, 256, 2>(a, sm_count, grid, work_stride);
+  if (rc || !a.symmetric) return rc;
+  if (a.n_end != 0 || a.state_in || a.state_dump || a.state_out)
+    return fail(RG_ERR_INVALID_ARG, "symmetric sweep: segment arguments are not supported");
+  int g2 = 0;
+  int64_t s2 = 0;
+  if ((rc = sweep_sym_plan(a, sm_count, &g2, &s2))) return rc;
+  *grid = std::max(*grid, g2);
+  *work_stride = std::max(*work_stride, s2);
+  return RG_OK;
 }
 
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  if (a.force_large) return launch_sweep_large(a, stream, grid);
-  if (a.max_M <= 16) return launch_t<16, 64, 8>(a, stream, grid);
-  if (a.max_M <= 32) return launch_t<32, 128, 4>(a, stream, grid);
-  if (a.max_M <= kMaxModesSmem) return launch_t<64, 256, 2>(a, stream, grid);
-  return launch_sweep_large(a, stream, grid);
+  if (a.force_large || a.max_M > kMaxModesSmem) return launch_sweep_large(a, stream, grid);
+  const SweepArgs* p = &a;
+  SweepArgs rerun;
+  if (a.symmetric) {
+    if (!a.flag_list) return fail(RG_ERR_INVALID_ARG, "symmetric sweep: no flag list");
+    int rc = launch_sweep_sym(a, stream, grid);
+    if (rc) return rc;
+    // The pivoted kernel takes the flagged items: queue length in counter 1,
+    // its own queue position in counter 2.
+    rerun = a;
+    rerun.symmetric = 0;
+    rerun.item_idx = a.flag_list;
+    rerun.count_ptr = a.work_counter + 1;
+    rerun.work_counter = a.work_counter + 2;
+    p = &rerun;
+  }
+  if (a.max_M <= 16) return launch_t<16, 64, 8>(*p, stream, grid);
+  if (a.max_M <= 32) return launch_t<32, 128, 4>(*p, stream, grid);
+  return launch_t<64, 256, 2>(*p, stream, grid);
 }
 
 int launch_histogram(const double* d_samples, int64_t n, const double* d_bins, int nbins,

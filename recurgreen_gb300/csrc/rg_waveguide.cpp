@@ -173,6 +173,9 @@ void jump_polynomial(uint64_t distance, uint64_t out[4]) {
 // ---------------------------------------------------------------------------
 // The waveguide handle.
 // ---------------------------------------------------------------------------
+// Entries of the argument set a cached batch graph was captured with.
+constexpr int kGraphKey = 12;
+
 struct rg_waveguide {
   rg_params p{};
   int nmu = 0, ny = 0, nx = 0, imin = 0, imax = 0, jmin = 0, jmax = 0, neigv = 0, nprop = 0;
@@ -196,10 +199,11 @@ struct rg_waveguide {
   size_t scratch_bytes = 0;
   cudaEvent_t ev_sweep0 = nullptr, ev_sweep1 = nullptr;  // around the last batch's sweep launches
   bool sweep_timed = false;
+  rg_batch_info last_batch{};  // launch configuration of the last batch (rerun read on demand)
   // The last batch launch, captured as a CUDA graph and replayed while its
   // arguments (sizes, buffers, workspace, kernel choice) stay the same.
   cudaGraphExec_t graph = nullptr;
-  int64_t graph_key[10] = {0};
+  int64_t graph_key[kGraphKey] = {0};
 };
 
 namespace {
@@ -386,7 +390,7 @@ int upload_tables(rg_waveguide* w) {
   if ((rc = upload(&w->d_costab, w->costab.data(), sizeof(double) * w->costab.size()))) return rc;
   if ((rc = upload(&w->d_expfac, w->expfac.data(), sizeof(double2) * w->expfac.size()))) return rc;
   if ((rc = upload(&w->d_jump, w->jump.data(), sizeof(uint64_t) * w->jump.size()))) return rc;
-  RG_CUDA(cudaMalloc((void**)&w->d_counter, sizeof(int)));
+  RG_CUDA(cudaMalloc((void**)&w->d_counter, sizeof(int) * rg::kQueueCounters));
   rg::WgDesc d{};
   d.M = w->nmu;
   d.ny = w->ny;
@@ -431,6 +435,21 @@ int ensure_scratch(rg_waveguide* w, size_t bytes) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// The symmetric sweep is on unless RG_SYMMETRIC=0; RG_SYM_TAU overrides its
+// pivot threshold (a huge value sends every item to the pivoted kernel).
+bool symmetric_enabled() {
+  const char* e = std::getenv("RG_SYMMETRIC");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+
+double symmetric_tau() {
+  const char* e = std::getenv("RG_SYM_TAU");
+  if (!e || !*e) return rg::kSymTau;
+  char* end = nullptr;
+  const double t = std::strtod(e, &end);
+  return (end && *end == '\0' && t >= 0.0) ? t : rg::kSymTau;
+}
+
 // Launch arguments for items of this one waveguide (the caller sets nreal,
 // seeds or upot, outputs and the workspace).
 rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
@@ -440,40 +459,47 @@ rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
   a.work_counter = w->d_counter;
   a.max_M = w->nmu;
   a.max_ny = w->ny;
+  a.symmetric = (w->p.boundtype == RG_BOUND_DIRICHLET && w->nmu <= rg::kMaxModesSmem && symmetric_enabled()) ? 1 : 0;
+  a.sym_tau = symmetric_tau();
   return a;
 }
 
 // Plans a launch, grows the scratch to hold `off` bytes plus the per-CTA
-// workspace, and sets a.work.  Pointers into the scratch below `off` must be
-// taken after this call (the scratch may move).
+// workspace (and the flag list of a symmetric sweep), and sets a.work and
+// a.flag_list.  Pointers into the scratch below `off` must be taken after
+// this call (the scratch may move).
 int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
   int64_t stride = 0;
   int rc = rg::sweep_plan(a, w->sm_count, grid, &stride);
   if (rc) return rc;
   const int slots = *grid / (a.cluster > 0 ? a.cluster : 1);  // one workspace per cluster
-  if ((rc = ensure_scratch(w, off + sizeof(double2) * (size_t)stride * slots))) return rc;
+  const size_t ws = align256(sizeof(double2) * (size_t)stride * slots);
+  const size_t fl = a.symmetric ? align256(sizeof(int32_t) * (size_t)a.nreal) : 0;
+  if ((rc = ensure_scratch(w, off + ws + fl))) return rc;
   a.work = (double2*)((char*)w->d_scratch + off);
   a.work_stride = stride;
+  a.flag_list = a.symmetric ? (int32_t*)((char*)w->d_scratch + off + ws) : nullptr;
   return RG_OK;
 }
 
 // ---------------------------------------------------------------------------
 // Autotuner.  For a waveguide shape (M, ny) and a batch size, the candidate
-// launch configurations -- the shared-memory kernel or the blocked kernel
-// for M <= 64, and the blocked kernel's cluster size (CTAs per realization)
-// -- are timed once on a short proxy guide (the same modes and grid, 16
+// launch configurations -- for M <= 64 the symmetric kernel (Dirichlet),
+// the pivoted shared-memory kernel or the blocked kernel, and above 64 modes
+// the blocked kernel's cluster size (CTAs per realization) -- are timed once on a short proxy guide (the same modes and grid, 16
 // slices, the same number of realizations) and the fastest is cached for the
 // process.  RG_AUTOTUNE=0 disables it (the built-in heuristics decide).
 // ---------------------------------------------------------------------------
 struct TuneChoice {
   int force_large = 0;
   int force_cluster = 0;
+  int general = 0;  // 1: the pivoted kernel even where the symmetric one applies
 };
 
 struct TuneKey {
-  int M, ny, bucket, sms;
+  int M, ny, bucket, sms, sym;
   bool operator<(const TuneKey& o) const {
-    return std::tie(M, ny, bucket, sms) < std::tie(o.M, o.ny, o.bucket, o.sms);
+    return std::tie(M, ny, bucket, sms, sym) < std::tie(o.M, o.ny, o.bucket, o.sms, o.sym);
   }
 };
 
@@ -502,20 +528,22 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
   a.status = d_status;
   a.force_large = tc.force_large;
   a.force_cluster = tc.force_cluster;
+  a.symmetric = a.symmetric && !tc.general;
   int grid = 0;
   int64_t stride = 0;
   if (rg::sweep_plan(a, w->sm_count, &grid, &stride) != RG_OK) return 1e30;
-  const size_t need = sizeof(double2) * (size_t)stride * (grid / (a.cluster > 0 ? a.cluster : 1));
+  const size_t need = align256(sizeof(double2) * (size_t)stride * (grid / (a.cluster > 0 ? a.cluster : 1)));
   double2* ws = nullptr;
-  if (cudaMalloc((void**)&ws, need) != cudaSuccess) {
+  if (cudaMalloc((void**)&ws, need + sizeof(int32_t) * (size_t)n) != cudaSuccess) {
     cudaGetLastError();
     return 1e30;
   }
   a.work = ws;
   a.work_stride = stride;
+  a.flag_list = a.symmetric ? (int32_t*)((char*)ws + need) : nullptr;
   double best = 1e30;
   for (int rep = 0; rep < 2; ++rep) {
-    cudaMemsetAsync(w->d_counter, 0, sizeof(int), s);
+    cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);
     cudaEventRecord(w->ev_sweep0, s);
     if (rg::launch_sweep(a, s, grid) != RG_OK) break;
     cudaEventRecord(w->ev_sweep1, s);
@@ -534,7 +562,8 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
 TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   TuneChoice def;
   if (!autotune_enabled() || n <= 0) return def;
-  const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count};
+  const int sym = make_args(w, rg::kModeEig).symmetric;
+  const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count, sym};
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
@@ -542,10 +571,11 @@ TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   }
   std::vector<TuneChoice> cands;
   if (w->nmu <= rg::kMaxModesSmem) {
-    cands.push_back(TuneChoice{0, 0});
-    if (w->nmu > 32) cands.push_back(TuneChoice{1, 1});
+    cands.push_back(TuneChoice{0, 0, 0});
+    if (sym) cands.push_back(TuneChoice{0, 0, 1});
+    if (w->nmu > 32) cands.push_back(TuneChoice{1, 1, 0});
   } else {
-    for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{1, c});
+    for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{1, c, 0});
   }
   if (cands.size() == 1) {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -605,16 +635,21 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   a.status = d_status;
   a.force_large = tc.force_large;
   a.force_cluster = tc.force_cluster;
+  a.symmetric = a.symmetric && !tc.general;
   int grid = 0, rc;
   if ((rc = place_workspace(w, a, 0, &grid))) return rc;
-  const int64_t key[10] = {n, (int64_t)(intptr_t)d_seeds, (int64_t)(intptr_t)d_teig, (int64_t)(intptr_t)d_status,
-                           (int64_t)(intptr_t)a.work, grid, a.cluster, a.force_large, a.work_stride, 1};
+  int64_t tau_bits = 0;
+  std::memcpy(&tau_bits, &a.sym_tau, sizeof tau_bits);
+  const int64_t key[kGraphKey] = {n, (int64_t)(intptr_t)d_seeds, (int64_t)(intptr_t)d_teig,
+                                  (int64_t)(intptr_t)d_status, (int64_t)(intptr_t)a.work, grid, a.cluster,
+                                  a.force_large, a.work_stride, a.symmetric, (int64_t)(intptr_t)a.flag_list,
+                                  tau_bits};
   if (!w->graph || std::memcmp(key, w->graph_key, sizeof key) != 0) {
     if (w->graph) cudaGraphExecDestroy(w->graph);
     w->graph = nullptr;
     cudaGraph_t gr = nullptr;
     RG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemsetAsync(w->d_counter, 0, sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);
     rc = (e == cudaSuccess) ? rg::launch_sweep(a, s, grid) : rg::cuda_fail(e, "graph capture");
     const cudaError_t ec = cudaStreamEndCapture(s, &gr);
     if (rc) {
@@ -632,6 +667,12 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   RG_CUDA(cudaGraphLaunch(w->graph, s));
   RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
   w->sweep_timed = true;
+  w->last_batch.kernel = (a.force_large || a.max_M > rg::kMaxModesSmem) ? RG_KERNEL_BLOCKED
+                         : a.symmetric                                 ? RG_KERNEL_SYMMETRIC
+                                                                       : RG_KERNEL_PIVOTED;
+  w->last_batch.grid = grid;
+  w->last_batch.cluster = a.cluster > 0 ? a.cluster : 1;
+  w->last_batch.rerun = 0;
   return RG_OK;
 }
 
@@ -655,7 +696,7 @@ const char* status_text(int code) {
 // G(x_1; x_1)).  The seed's potential is drawn inside the kernel, except for
 // r, whose reverse sweep needs the rows in reverse order: then it is drawn
 // into scratch first.  Scratch layout: [potential | t | r | eigenvalues |
-// status | seed | per-CTA workspace].
+// status | seed | per-CTA workspace | flag list].
 int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int mode, double* h_teig,
                double* h_t, double* h_tfilt, double* h_r = nullptr) {
   DeviceGuard g(w->device);
@@ -709,14 +750,14 @@ int run_single(rg_waveguide* w, const int32_t* seed, const double* h_upot, int m
   a.tout = (h_t || h_tfilt) ? d_t : nullptr;
   a.teig = d_teig;
   a.status = d_status;
-  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s));
   if ((rc = rg::launch_sweep(a, s, grid))) return rc;
   if (want_r) {
     rg::SweepArgs b = a;
     b.mode = rg::kModeRefl;
     b.tout = d_r;
     b.status = d_status + 1;
-    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+    RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s));
     if ((rc = rg::launch_sweep(b, s, grid))) return rc;
   }
   int32_t st[2] = {0, 0};
@@ -746,6 +787,9 @@ int noalloc_view(const rg_waveguide* w, NoAllocView* out) {
   out->jumppoly = w->d_jump;
   out->stream = w->stream;
   out->d_desc = w->d_desc;
+  const SweepArgs a = make_args(w, kModeEig);
+  out->symmetric = a.symmetric;
+  out->sym_tau = a.sym_tau;
   return RG_OK;
 }
 
@@ -1032,9 +1076,15 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     a.work_counter = w0->d_counter;
     a.max_M = maxM;
     a.max_ny = maxny;
+    // The symmetric kernel when the class has Dirichlet items (it hands
+    // periodic ones straight to the pivoted kernel).
+    bool any_dirichlet = false;
+    for (int k = k0; k < k1; ++k) any_dirichlet = any_dirichlet || !descs[o_wg[k]].periodic;
+    a.symmetric = (maxM <= rg::kMaxModesSmem && any_dirichlet && symmetric_enabled()) ? 1 : 0;
+    a.sym_tau = symmetric_tau();
     int grid = 0;
     if ((rc = place_workspace(w0, a, 0, &grid))) break;
-    e = cudaMemsetAsync(w0->d_counter, 0, sizeof(int), s);
+    e = cudaMemsetAsync(w0->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);
     if (e != cudaSuccess) {
       rc = rg::cuda_fail(e, "rg_tdistrib_multi counter");
       break;
@@ -1075,6 +1125,7 @@ int rg_sweep_segment(rg_waveguide* w, const double* d_upot, int n, int n_begin, 
   rg::SweepArgs a = make_args(w, rg::kModeEig);
   a.nreal = n;
   a.force_large = 1;
+  a.symmetric = 0;
   a.upot = d_upot;
   a.pot_rstride = (int64_t)w->p.nxdiso * w->ny;
   a.pot_xstride = w->ny;
@@ -1089,7 +1140,7 @@ int rg_sweep_segment(rg_waveguide* w, const double* d_upot, int n, int n_begin, 
   a.status = d_status;
   int grid = 0, rc;
   if ((rc = place_workspace(w, a, 0, &grid))) return rc;
-  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int), s));
+  RG_CUDA(cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s));
   return rg::launch_sweep(a, s, grid);
 }
 
@@ -1106,10 +1157,25 @@ int rg_adjoint_grad_rows(rg_waveguide* w, const double* d_xbar, int n, double* d
 
 int rg_last_sweep_time(rg_waveguide* w, float* ms) {
   if (!w || !ms) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_sweep_time: NULL argument");
-  if (!w->sweep_timed) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_sweep_time: no single-launch batch timed yet");
+  if (!w->sweep_timed) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_sweep_time: no batch timed yet");
   DeviceGuard g(w->device);
   RG_CUDA(cudaEventSynchronize(w->ev_sweep1));
   RG_CUDA(cudaEventElapsedTime(ms, w->ev_sweep0, w->ev_sweep1));
+  return RG_OK;
+}
+
+int rg_last_batch_info(rg_waveguide* w, rg_batch_info* info) {
+  if (!w || !info) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_batch_info: NULL argument");
+  if (!w->sweep_timed) return rg::fail(RG_ERR_INVALID_ARG, "rg_last_batch_info: no batch run yet");
+  DeviceGuard g(w->device);
+  RG_CUDA(cudaEventSynchronize(w->ev_sweep1));
+  *info = w->last_batch;
+  if (info->kernel == RG_KERNEL_SYMMETRIC) {
+    int32_t flagged = 0;
+    RG_CUDA(cudaMemcpyAsync(&flagged, w->d_counter + 1, sizeof flagged, cudaMemcpyDeviceToHost, w->stream));
+    RG_CUDA(cudaStreamSynchronize(w->stream));
+    info->rerun = flagged;
+  }
   return RG_OK;
 }
 
