@@ -12,15 +12,30 @@ Metric: realizations/s (higher is better).  `value` is device-timed with the
 seeds already in HBM; `e2e` goes through the C ABI with host buffers
 (seeds copied in, eigenvalues and statuses copied out, inside the timing).
 
+`per_realization` times the drop-in path on a few of the same seeds: one
+rg_compute_tdistrib call per seed (the reference's unit of work,
+src/main.f90:156), so `batched_over_per_realization` is the batching gain.
+
 `--impl reference` times the reference's CPU algorithm (the oracle's C
 restatement with LAPACK, OpenMP over seeds) on all host cores, on a bounded
 sample of the same workload; gfortran is absent so the Fortran program itself
 cannot be built here.
+
+`--workload` selects a secondary measurement instead of the default line:
+  n256   M=256 modes (kW/pi=256.5, wol=128.25), Nx=2000, ny=1024: batched
+         (--batch realizations, default 152) vs per-realization calls;
+  uneven 2048 guides with N in {32,...,256}, Nx in [500,5000], L/l_s in
+         [1,20], absorption on half (numpy default_rng(0)), ny=4N, through
+         rg_tdistrib_multi, plus per-N histograms;
+  diff   M=128, Nx=1000, ny=512, 256 realizations: Tr(t^H t), Tr((t^H t)^2)
+         and both gradients w.r.t. U through the adjoint sweep;
+  large  M=512, Nx=10^4 (or --nx), ny=2048, --batch realizations (default 19).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -177,6 +192,141 @@ def run_reference(args) -> None:
     print(json.dumps(out))
 
 
+def _sync_time(torch, fn):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, r
+
+
+def _per_realization(L, w, seeds, np) -> tuple[float, float]:
+    """Drop-in path: one rg_compute_tdistrib call per seed; (realizations/s, seconds)."""
+    import ctypes
+
+    tall = np.zeros(max(seeds) * w.neigv)
+    dp = ctypes.POINTER(ctypes.c_double)
+    t0 = time.perf_counter()
+    for s in seeds:
+        rc = L.rg_compute_tdistrib(w._h, int(s), tall.ctypes.data_as(dp), tall.size)
+        if rc:
+            raise RuntimeError(L.rg_last_error().decode())
+    dt = time.perf_counter() - t0
+    return len(seeds) / dt, dt
+
+
+def run_workload(args) -> None:
+    """Secondary measurements (one JSON line each); see the module docstring."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import recurgreen_gb300 as rg
+
+    torch.cuda.init()
+    L = rg.lib()
+    out = {"workload": args.workload, "dtype": "f64", "data": "synthetic", "n_gpus": 1}
+    peak, peak_src = measured_fp64_peak(torch)
+    out["fp64_peak_tflops"] = peak
+    out["fp64_peak_source"] = peak_src
+    if args.workload in ("n256", "large"):
+        if args.workload == "n256":
+            kw = dict(WORKLOAD, wol=128.25, nxdiso=args.nx, ny=1024)
+            n = args.batch if args.batch != NSEED else 152
+        else:
+            kw = dict(WORKLOAD, wol=256.25, nxdiso=args.nx if args.nx != 2000 else 10000, dscat=20.0, ny=2048)
+            n = args.batch if args.batch != NSEED else 19
+        w = rg.Waveguide(**kw)
+        seeds = np.arange(1, n + 1, dtype=np.int32)
+        # warm-up: the autotuner's choice depends on (modes, ny, batch size), not on
+        # Nx, so a 16-slice copy of the guide tunes this batch outside the timing
+        rg.Waveguide(**dict(kw, nxdiso=16)).tdistrib_batch(seeds)
+        times = []
+        for _ in range(max(args.steps, 1)):
+            dt, _ = _sync_time(torch, lambda: w.tdistrib_batch(seeds))
+            times.append(dt)
+        ms = ctypes.c_float()
+        L.rg_last_sweep_time(w._h, ctypes.byref(ms))
+        info = w.last_batch_info()
+        dt = min(times)
+        fl = flops_per_realization(w.nmu, w.nx)
+        out.update({"modes": w.nmu, "nx": w.nx, "ny": w.ny, "realizations": n, "launch": info,
+                    "batched_realizations_per_s": n / dt, "batched_seconds": dt,
+                    "sweep_kernel_seconds": ms.value / 1e3,
+                    "dense_equivalent_tflops": fl * n / (ms.value / 1e3) / 1e12})
+        out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
+        if args.per_sample > 0:
+            pr, pdt = _per_realization(L, w, list(range(1, args.per_sample + 1)), np)
+            out["per_realization_per_s"] = pr
+            out["per_realization_sample"] = f"{args.per_sample} seeds, one rg_compute_tdistrib call each, {pdt:.1f} s"
+            out["batched_over_per_realization"] = out["batched_realizations_per_s"] / pr
+    elif args.workload == "uneven":
+        rng = np.random.default_rng(0)
+        Ns = [32, 48, 64, 96, 128, 192, 256]
+        n = args.batch if args.batch != NSEED else 2048
+        guides, items, fl = {}, [], 0.0
+        t0 = time.perf_counter()
+        for k in range(n):
+            N = int(rng.choice(Ns))
+            nx = int(rng.integers(500, 5001))
+            ds = float(rng.uniform(1, 20))
+            wol = (N + 0.5) / 2
+            dabso = 0.02 * math.pi * wol if rng.random() < 0.5 else 0.0
+            g = rg.Waveguide("dirichlet", nxdiso=nx, nxfree=0, wol=wol, exfac=1.0, aratio=1.0, dscat=ds,
+                             dabso=dabso, ny=4 * N)
+            guides[k] = g
+            items.append((g, k + 1))
+            fl += flops_per_realization(g.nmu, nx)
+        t_init = time.perf_counter() - t0
+        dt, (res, st) = _sync_time(torch, lambda: rg.tdistrib_multi(items, return_status=True))
+        # per-N histograms of T on the tdistrib task's Chebyshev edges (src/main.f90:233)
+        from recurgreen_gb300.tdistrib import chebyshev_bins
+        t1 = time.perf_counter()
+        hist = {}
+        for N in Ns:
+            sel = [T for (g, _), T in zip(items, res) if g.nmu == N]
+            if sel:
+                h, miss = rg.histogram(np.concatenate(sel), chebyshev_bins(100))
+                hist[N] = {"guides": len(sel), "samples": int(sum(x.size for x in sel)), "missing": miss}
+        t_hist = time.perf_counter() - t1
+        out.update({"guides": n, "guides_per_s": n / dt, "seconds": dt, "init_seconds": t_init,
+                    "histogram_seconds": t_hist, "bad_status": int((st != 0).sum()),
+                    "dense_equivalent_tflops": fl / dt / 1e12, "total_tflop": fl / 1e12, "per_N": hist})
+        out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
+    elif args.workload == "diff":
+        from recurgreen_gb300.adjoint import transmission_losses
+
+        kw = dict(WORKLOAD, wol=64.25, nxdiso=args.nx if args.nx != 2000 else 1000, dscat=5.0, ny=512)
+        w = rg.Waveguide(**kw)
+        n = args.batch if args.batch != NSEED else 256
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(0)
+        U = (torch.randn(n, w.nxdiso, w.ny, dtype=torch.float64, device="cuda", generator=gen) * w.stdu)
+        U.requires_grad_(True)
+        K = max(1, int(round(math.sqrt(w.nx))))
+
+        def fwd():
+            return transmission_losses(U, w, K)
+
+        def step():
+            L1, L2 = transmission_losses(U, w, K)
+            g1, = torch.autograd.grad(L1.sum(), U, retain_graph=True)
+            g2, = torch.autograd.grad(L2.sum(), U)
+            return g1, g2
+
+        fwd()
+        t_fwd, _ = _sync_time(torch, fwd)
+        t_all, (g1, g2) = _sync_time(torch, step)
+        fl = flops_per_realization(w.nmu, w.nx)
+        out.update({"modes": w.nmu, "nx": w.nx, "ny": w.ny, "realizations": n, "checkpoint_every": K,
+                    "forward_seconds": t_fwd, "forward_and_two_gradients_seconds": t_all,
+                    "realizations_per_s_with_gradients": n / t_all,
+                    "forward_dense_equivalent_tflops": fl * n / t_fwd / 1e12,
+                    "gradient_finite": bool(torch.isfinite(g1).all().item() and torch.isfinite(g2).all().item())})
+    print(json.dumps(out))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,11 +339,18 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nx", type=int, default=WORKLOAD["nxdiso"],
                     help="slices (profiling runs only; the workload is Nx=2000)")
+    ap.add_argument("--per-sample", type=int, default=4,
+                    help="seeds timed through the per-realization drop-in call (0: skip)")
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "n256", "uneven", "diff", "large"])
     args = ap.parse_args()
-    WORKLOAD["nxdiso"] = args.nx
     if args.impl == "reference":
+        WORKLOAD["nxdiso"] = args.nx
         run_reference(args)
         return
+    if args.workload != "uniform":
+        run_workload(args)
+        return
+    WORKLOAD["nxdiso"] = args.nx
 
     import numpy as np
     import torch
@@ -270,6 +427,12 @@ def main() -> None:
         t = torch.tensor([e2e_dt], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_dt = float(t.item())
+    per = None
+    if args.per_sample > 0 and rank == 0:
+        pr, pdt = _per_realization(L, w, list(seeds_h[: args.per_sample]), np)
+        per = {"value": pr, "unit": UNIT,
+               "sample": f"seeds {int(seeds_h[0])}..{int(seeds_h[min(args.per_sample, n) - 1])}, one "
+                         f"rg_compute_tdistrib call each (host buffers, one CTA per call), {pdt:.1f} s"}
 
     info = w.last_batch_info()
     fl = flops_per_realization(w.nmu, w.nx)
@@ -300,6 +463,9 @@ def main() -> None:
                            "kernel_timing": "CUDA events around the sweep launch" if len(sweep_ms) == args.steps
                            else "whole step (potential + sweep)"}
         out["slice_solves_per_s"] = value * (w.nx)
+        if per:
+            out["per_realization"] = per
+            out["batched_over_per_realization"] = value / per["value"]
         if clocks:
             out["clocks"] = clocks
         if not args.no_cpu:

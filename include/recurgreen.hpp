@@ -1,0 +1,216 @@
+/*
+ * recurgreen.hpp -- C++ host interface over the C ABI of recurgreen.h.
+ *
+ * recurgreen::Waveguide mirrors the reference's `type(waveguide_t)`
+ * (src/waveguide.f90:13-73): the constructor is `init`, the copy constructor
+ * `init_copy`, the destructor `del`, and the type-bound procedures keep their
+ * names (get_nmu, get_neigv, get_nx, get_xmesh, get_parameters,
+ * compute_tdistrib, compute_refl_trans_v1, print_parameters,
+ * generate_directory).  Where the reference prints a message and stops
+ * (src/base_utils.f90:56-57), these methods throw recurgreen::Error carrying
+ * the library's status code and message.  Header-only; link against
+ * librecurgreen_gb300.so.
+ */
+#ifndef RECURGREEN_HPP
+#define RECURGREEN_HPP
+
+#include <complex>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "recurgreen.h"
+
+namespace recurgreen {
+
+class Error : public std::runtime_error {
+ public:
+  Error(int code, const std::string& msg) : std::runtime_error(msg), code_(code) {}
+  int code() const { return code_; }
+
+ private:
+  int code_;
+};
+
+inline void check(int rc) {
+  if (rc != RG_OK) throw Error(rc, rg_last_error());
+}
+
+// The `&waveguide` namelist (src/main.f90:83) plus the transverse grid size ny
+// (0: the reference's ny = nmu).
+struct Parameters {
+  std::string boundtype = "dirichlet";
+  int nxdiso = 0, nxfree = 0;
+  double wol = 0, exfac = 1, aratio = 1, dscat = 0, dabso = 0, napera = 1, naperb = 1;
+  int ny = 0;
+};
+
+// Fortran F0.d as gfortran writes it: no field width, so a value below one
+// in magnitude has no leading zero (0.2 -> ".200000", -0.5 -> "-.500000").
+inline std::string format_f0(double x, int d = 6) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.*f", d, x);
+  std::string s = buf;
+  if (s.rfind("0.", 0) == 0) return s.substr(1);
+  if (s.rfind("-0.", 0) == 0) return "-" + s.substr(2);
+  return s;
+}
+
+class Waveguide {
+ public:
+  // init (src/waveguide.f90:81-85): validates the parameters with the
+  // reference's messages and builds the waveguide on the current CUDA device.
+  explicit Waveguide(const Parameters& p) {
+    rg_params c{};
+    if (p.boundtype == "dirichlet") {
+      c.boundtype = RG_BOUND_DIRICHLET;
+    } else if (p.boundtype == "periodic") {
+      c.boundtype = RG_BOUND_PERIODIC;
+    } else {
+      c.boundtype = -1;  // rejected by rg_init with the reference's message
+    }
+    c.nxdiso = p.nxdiso;
+    c.nxfree = p.nxfree;
+    c.wol = p.wol;
+    c.exfac = p.exfac;
+    c.aratio = p.aratio;
+    c.dscat = p.dscat;
+    c.dabso = p.dabso;
+    c.napera = p.napera;
+    c.naperb = p.naperb;
+    c.ny = p.ny;
+    check(rg_init(&c, &h_));
+  }
+  // init_copy (src/waveguide.f90:262-270).
+  Waveguide(const Waveguide& o) { check(rg_init_copy(o.h_, &h_)); }
+  Waveguide& operator=(const Waveguide& o) {
+    if (this != &o) {
+      rg_waveguide* n = nullptr;
+      check(rg_init_copy(o.h_, &n));
+      rg_del(h_);
+      h_ = n;
+    }
+    return *this;
+  }
+  Waveguide(Waveguide&& o) noexcept : h_(o.h_) { o.h_ = nullptr; }
+  Waveguide& operator=(Waveguide&& o) noexcept {
+    if (this != &o) {
+      rg_del(h_);
+      h_ = o.h_;
+      o.h_ = nullptr;
+    }
+    return *this;
+  }
+  // del (src/waveguide.f90:275-286).
+  ~Waveguide() { rg_del(h_); }
+
+  rg_waveguide* handle() const { return h_; }
+
+  // Getters (src/waveguide.f90:291-350) and the derived sizes.
+  int get_nmu() const { return rg_get_nmu(h_); }
+  int get_neigv() const { return rg_get_neigv(h_); }
+  int get_nx() const { return rg_get_nx(h_); }
+  int get_ny() const { return rg_get_ny(h_); }
+  int get_nprop() const { return rg_get_nprop(h_); }
+  void get_window(int* imin, int* imax, int* jmin, int* jmax) const {
+    check(rg_get_window(h_, imin, imax, jmin, jmax));
+  }
+  std::vector<double> get_xmesh() const {
+    std::vector<double> x(get_nx());
+    check(rg_get_xmesh(h_, x.data(), (int64_t)x.size()));
+    return x;
+  }
+  Parameters get_parameters() const {
+    rg_params c{};
+    check(rg_get_parameters(h_, &c));
+    Parameters p;
+    p.boundtype = c.boundtype == RG_BOUND_PERIODIC ? "periodic" : "dirichlet";
+    p.nxdiso = c.nxdiso;
+    p.nxfree = c.nxfree;
+    p.wol = c.wol;
+    p.exfac = c.exfac;
+    p.aratio = c.aratio;
+    p.dscat = c.dscat;
+    p.dabso = c.dabso;
+    p.napera = c.napera;
+    p.naperb = c.naperb;
+    p.ny = c.ny;
+    return p;
+  }
+
+  // compute_tdistrib (src/waveguide.f90:392-462): chunk iseed of tallvals.
+  void compute_tdistrib(int iseed, std::vector<double>& tallvals) {
+    check(rg_compute_tdistrib(h_, iseed, tallvals.data(), (int64_t)tallvals.size()));
+  }
+  // compute_refl_trans_v1 (src/waveguide.f90:469-519): nmu x nmu, column-major.
+  void compute_refl_trans_v1(int iseed, std::vector<std::complex<double>>& rmat,
+                             std::vector<std::complex<double>>& tmat) {
+    const size_t n = (size_t)get_nmu() * get_nmu();
+    rmat.resize(n);
+    tmat.resize(n);
+    check(rg_compute_refl_trans_v1(h_, iseed, reinterpret_cast<double*>(rmat.data()),
+                                   reinterpret_cast<double*>(tmat.data())));
+  }
+  // The seed loop of src/main.f90:134-179 as one batched launch: neigv
+  // eigenvalues per seed, in seed order.  Throws on the first bad status
+  // unless `status` is given (then every realization's status is returned).
+  std::vector<double> tdistrib_batch(const std::vector<int32_t>& seeds, std::vector<int32_t>* status = nullptr) {
+    std::vector<double> out(seeds.size() * (size_t)get_neigv());
+    std::vector<int32_t> st(seeds.size());
+    const int rc = rg_tdistrib_batch(h_, seeds.data(), (int)seeds.size(), out.data(), st.data());
+    if (status) {
+      *status = st;
+      if (rc != RG_OK && rc != RG_ERR_SINGULAR && rc != RG_ERR_NOCONV) check(rc);
+    } else {
+      check(rc);
+    }
+    return out;
+  }
+
+  // print_parameters (src/waveguide.f90:1003-1018): three lines, each
+  // starting with `prefix`.
+  void print_parameters(std::FILE* fp, const std::string& prefix) const {
+    const Parameters p = get_parameters();
+    int imin, imax, jmin, jmax;
+    get_window(&imin, &imax, &jmin, &jmax);
+    std::fprintf(fp, "%s Waveguide 2D with boundtype='%s', W/lambda=%s, exfac=%s, Nmode=%d, Nprop=%d\n",
+                 prefix.c_str(), p.boundtype.c_str(), format_f0(p.wol).c_str(), format_f0(p.exfac).c_str(),
+                 get_nmu(), get_nprop());
+    std::fprintf(fp, "%s Filtering: NAper_a=%s (Nmode_a=%d), NAper_b=%s (Nmode_b=%d), Neigv=%d\n", prefix.c_str(),
+                 format_f0(p.napera).c_str(), jmax - jmin + 1, format_f0(p.naperb).c_str(), imax - imin + 1,
+                 get_neigv());
+    std::fprintf(fp, "%s Medium: L/lscat=%s, L/labso=%s, Nx_diso=%d, Nx_free=%d, aratio=L/W=%s\n",
+                 prefix.c_str(), format_f0(p.dscat).c_str(), format_f0(p.dabso).c_str(), p.nxdiso, p.nxfree,
+                 format_f0(p.aratio).c_str());
+  }
+
+  // generate_directory (src/waveguide.f90:1046-1067): root/dscat_X/dabso_Y/wol_Z/boundtype/
+  // with X, Y, Z written as F0.6 and trailing zeros removed.
+  std::string generate_directory(const std::string& root = "out") const {
+    const Parameters p = get_parameters();
+    auto folder = [](const char* stem, double v) {
+      std::string s = std::string(stem) + (v < 1.0 ? "0" : "") + format_f0(v);
+      while (!s.empty() && (s.back() == '0' || s.back() == ' ')) s.pop_back();
+      return s;
+    };
+    return root + "/" + folder("dscat_", p.dscat) + "/" + folder("dabso_", p.dabso) + "/" + folder("wol_", p.wol) +
+           "/" + p.boundtype + "/";
+  }
+
+ private:
+  rg_waveguide* h_ = nullptr;
+};
+
+// histogram (src/base_utils.f90:491-516) on the GPU: counts of samples in
+// the nbins = bins.size() - 1 intervals, and the number of missing samples.
+inline std::vector<double> histogram(const std::vector<double>& samples, const std::vector<double>& bins,
+                                     double* missing) {
+  std::vector<double> h(bins.size() > 0 ? bins.size() - 1 : 0);
+  check(rg_histogram(samples.data(), (int64_t)samples.size(), bins.data(), (int)h.size(), h.data(), missing));
+  return h;
+}
+
+}  // namespace recurgreen
+
+#endif  // RECURGREEN_HPP

@@ -1,8 +1,11 @@
-"""Builds librecurgreen_gb300.so (the C ABI of include/recurgreen.h) in-tree.
+"""Builds librecurgreen_gb300.so (the C ABI of include/recurgreen.h) in-tree,
+and the host programs bin/recurgreen and bin/plothisto on top of it.
 
-nvcc compiles every translation unit for sm_103a only (one -gencode), in
+nvcc compiles every CUDA translation unit for sm_103a only (one -gencode), in
 parallel, then links a shared library with the CUDA runtime linked
 statically, so the library has no run-time dependency beyond the driver.
+The host programs are plain C++17 (g++), linked against the library with an
+rpath to it.
 """
 from __future__ import annotations
 
@@ -17,6 +20,10 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librecurgreen_gb300.so")
+HOST = os.path.join(PKG, "host")
+BIN = os.path.join(PKG, "bin")
+HOST_SOURCES = ["driver.cpp"]
+PROGRAMS = {"recurgreen": "recurgreen_main.cpp", "plothisto": "plothisto_main.cpp"}
 SOURCES = ["rg_sweep.cu", "rg_sweep_sym.cu", "rg_sweep_large.cu", "rg_adjoint.cu", "rg_waveguide.cpp", "rg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -65,7 +72,34 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart=static", "-o", LIB] + objs
         run(cmd)
+    build_programs(force, run)
     return LIB
+
+
+def cxx() -> str:
+    cand = shutil.which("g++") or shutil.which("c++")
+    if not cand:
+        raise RuntimeError("g++ not found")
+    return cand
+
+
+def build_programs(force: bool, run) -> None:
+    """bin/recurgreen and bin/plothisto (host C++ over include/recurgreen.hpp)."""
+    os.makedirs(BIN, exist_ok=True)
+    hdrs = [os.path.join(ROOT, "include", "recurgreen.h"), os.path.join(ROOT, "include", "recurgreen.hpp"),
+            os.path.join(HOST, "driver.hpp")]
+    flags = ["-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include")]
+    objs = []
+    for src in HOST_SOURCES:
+        s, o = os.path.join(HOST, src), os.path.join(OBJ, "host_" + src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            run([cxx()] + flags + ["-c", s, "-o", o])
+    for prog, src in PROGRAMS.items():
+        s, exe = os.path.join(HOST, src), os.path.join(BIN, prog)
+        if force or _stale(exe, [s, LIB] + objs + hdrs):
+            run([cxx()] + flags + [s] + objs + ["-o", exe, "-L", PKG, "-lrecurgreen_gb300",
+                                                "-Wl,-rpath,$ORIGIN/.."])
 
 
 if __name__ == "__main__":

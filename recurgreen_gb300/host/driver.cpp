@@ -1,0 +1,617 @@
+// The `recurgreen` and `plothisto` drivers (see driver.hpp).
+#include "driver.hpp"
+
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cctype>
+#include <cerrno>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <limits>
+#include <sstream>
+
+#include "recurgreen.hpp"
+
+namespace rgdriver {
+
+namespace {
+
+const char* kProgram = "RecurGreen-GB300 (recursive Green sweep on GB300)";
+const char* kStopMessage = "RecurGreen: Invalid arguments, aborting...";
+
+std::string lower(std::string s) {
+  for (char& c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+
+std::string strip(const std::string& s) {
+  size_t a = 0, b = s.size();
+  while (a < b && std::isspace((unsigned char)s[a])) ++a;
+  while (b > a && std::isspace((unsigned char)s[b - 1])) --b;
+  return s.substr(a, b - a);
+}
+
+bool is_ident_start(char c) { return std::isalpha((unsigned char)c) || c == '_'; }
+bool is_ident(char c) { return std::isalnum((unsigned char)c) || c == '_'; }
+
+// A namelist body with the source line of every character.
+struct Body {
+  std::string text;
+  std::vector<int> line;  // index into `lines`
+};
+
+[[noreturn]] void invalid_entry(const std::string& line) {
+  throw Stop("Invalid entry in namelist: " + strip(line) + "...");
+}
+
+// Fortran real (list-directed): [sign] digits [. digits] [(e|d) [sign] digits],
+// or nan / inf / infinity.
+bool parse_real(const std::string& tok, double* out) {
+  std::string t = lower(strip(tok));
+  if (t.empty()) return false;
+  std::string u = (t[0] == '+' || t[0] == '-') ? t.substr(1) : t;
+  const double sign = (t[0] == '-') ? -1.0 : 1.0;
+  if (u == "nan") {
+    *out = std::numeric_limits<double>::quiet_NaN();
+    return true;
+  }
+  if (u == "inf" || u == "infinity") {
+    *out = sign * std::numeric_limits<double>::infinity();
+    return true;
+  }
+  size_t i = 0, nd = 0;
+  while (i < u.size() && std::isdigit((unsigned char)u[i])) ++i, ++nd;
+  if (i < u.size() && u[i] == '.') {
+    ++i;
+    while (i < u.size() && std::isdigit((unsigned char)u[i])) ++i, ++nd;
+  }
+  if (nd == 0) return false;
+  std::string num = u.substr(0, i);
+  if (i < u.size()) {
+    if (u[i] != 'e' && u[i] != 'd') return false;
+    size_t j = i + 1;
+    if (j < u.size() && (u[j] == '+' || u[j] == '-')) ++j;
+    const size_t k0 = j;
+    while (j < u.size() && std::isdigit((unsigned char)u[j])) ++j;
+    if (j == k0 || j != u.size()) return false;
+    num += "e" + u.substr(i + 1);
+  }
+  char* end = nullptr;
+  const double v = std::strtod(num.c_str(), &end);
+  if (!end || *end != '\0') return false;
+  *out = sign * v;
+  return true;
+}
+
+bool parse_int(const std::string& tok, long* out) {
+  const std::string t = strip(tok);
+  size_t i = (!t.empty() && (t[0] == '+' || t[0] == '-')) ? 1 : 0;
+  if (i >= t.size()) return false;
+  for (size_t j = i; j < t.size(); ++j)
+    if (!std::isdigit((unsigned char)t[j])) return false;
+  errno = 0;
+  const long v = std::strtol(t.c_str(), nullptr, 10);
+  if (errno) return false;
+  *out = v;
+  return true;
+}
+
+const NmlValue* find(const NmlGroup& g, const std::string& key) {
+  auto it = g.find(key);
+  return it == g.end() ? nullptr : &it->second;
+}
+
+std::string timestamp() {
+  std::time_t now = std::time(nullptr);
+  std::tm lt{};
+  localtime_r(&now, &lt);
+  char buf[64];
+  std::strftime(buf, sizeof buf, "%Y-%m-%d at %H:%M:%S %z", &lt);
+  return buf;
+}
+
+std::string fmt_int(long v) { return std::to_string(v); }
+
+// Fortran F0.d, including the F0.0 form "3." (a decimal point always).
+std::string f0(double x, int d) {
+  std::string s = recurgreen::format_f0(x, d);
+  if (d == 0) s += ".";
+  return s;
+}
+
+void write_rows(std::FILE* fp, const Density& d) {
+  for (size_t j = 0; j < d.rho.size(); ++j)
+    std::fprintf(fp, "%s, %s\n", format_g0(d.centre[j]).c_str(), format_g0(d.rho[j]).c_str());
+}
+
+std::string read_file(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  std::ostringstream ss;
+  ss << f.rdbuf();
+  return ss.str();
+}
+
+bool file_exists(const std::string& path) {
+  struct stat st;
+  return ::stat(path.c_str(), &st) == 0;
+}
+
+}  // namespace
+
+std::string tag_info() { return "[INFO] "; }
+std::string tag_warn() {
+  return isatty(STDOUT_FILENO) ? "[\033[1m\033[93mWARN\033[0m] " : "[WARN] ";
+}
+std::string tag_error() {
+  return isatty(STDERR_FILENO) ? "[\033[1m\033[31mERROR\033[0m] " : "[ERROR] ";
+}
+
+NmlGroup read_namelist(const std::string& text, const std::string& name, const std::vector<std::string>& allowed) {
+  // Lines without comments (`!` outside quotes).
+  std::vector<std::string> lines;
+  {
+    std::istringstream in(text);
+    std::string raw;
+    while (std::getline(in, raw)) {
+      if (!raw.empty() && raw.back() == '\r') raw.pop_back();
+      std::string out;
+      char q = 0;
+      for (char c : raw) {
+        if (q) {
+          out += c;
+          if (c == q) q = 0;
+        } else if (c == '\'' || c == '"') {
+          q = c;
+          out += c;
+        } else if (c == '!') {
+          break;
+        } else {
+          out += c;
+        }
+      }
+      lines.push_back(out);
+    }
+  }
+  const std::string want = "&" + lower(name);
+  size_t start = lines.size();
+  size_t col = 0;
+  for (size_t k = 0; k < lines.size(); ++k) {
+    const std::string s = lines[k];
+    size_t a = 0;
+    while (a < s.size() && std::isspace((unsigned char)s[a])) ++a;
+    if (lower(s.substr(a, want.size())) == want &&
+        (a + want.size() == s.size() || !is_ident(s[a + want.size()]))) {
+      start = k;
+      col = a + want.size();
+      break;
+    }
+  }
+  if (start == lines.size())
+    throw Stop("Invalid entry in namelist: group &" + name + " not found...\n" + tag_warn() +
+               "Try checking the spelling of the namelist groups...");
+  // Body up to the terminating `/` outside quotes.
+  Body body;
+  bool closed = false;
+  for (size_t k = start; k < lines.size() && !closed; ++k) {
+    const std::string& s = lines[k];
+    char q = 0;
+    for (size_t c = (k == start ? col : 0); c < s.size(); ++c) {
+      const char ch = s[c];
+      if (q) {
+        if (ch == q) q = 0;
+      } else if (ch == '\'' || ch == '"') {
+        q = ch;
+      } else if (ch == '/') {
+        closed = true;
+        break;
+      }
+      body.text += ch;
+      body.line.push_back((int)k);
+    }
+    body.text += '\n';
+    body.line.push_back((int)k);
+  }
+  if (!closed) invalid_entry(lines.back());
+  // Entries.
+  NmlGroup g;
+  const std::string& t = body.text;
+  size_t i = 0;
+  auto skip_sep = [&](size_t p) {
+    while (p < t.size() && (std::isspace((unsigned char)t[p]) || t[p] == ',')) ++p;
+    return p;
+  };
+  auto starts_entry = [&](size_t p) {  // identifier, spaces, '='
+    if (p >= t.size() || !is_ident_start(t[p])) return false;
+    while (p < t.size() && is_ident(t[p])) ++p;
+    while (p < t.size() && std::isspace((unsigned char)t[p])) ++p;
+    return p < t.size() && t[p] == '=';
+  };
+  for (i = skip_sep(i); i < t.size(); i = skip_sep(i)) {
+    const std::string& src = lines[body.line[i]];
+    if (!is_ident_start(t[i])) invalid_entry(src);
+    size_t j = i;
+    while (j < t.size() && is_ident(t[j])) ++j;
+    const std::string key = lower(t.substr(i, j - i));
+    while (j < t.size() && std::isspace((unsigned char)t[j])) ++j;
+    if (j >= t.size() || t[j] != '=') invalid_entry(src);
+    bool ok = false;
+    for (const auto& a : allowed) ok = ok || a == key;
+    if (!ok) invalid_entry(src);
+    NmlValue v;
+    v.line = src;
+    i = j + 1;
+    for (;;) {
+      while (i < t.size() && std::isspace((unsigned char)t[i])) ++i;
+      if (i >= t.size()) break;
+      if (t[i] == ',') {
+        ++i;
+        continue;
+      }
+      if (starts_entry(i)) break;
+      std::string item;
+      if (t[i] == '\'' || t[i] == '"') {
+        const char q = t[i++];
+        while (i < t.size()) {
+          if (t[i] == q) {
+            if (i + 1 < t.size() && t[i + 1] == q) {  // doubled quote
+              item += q;
+              i += 2;
+              continue;
+            }
+            ++i;
+            break;
+          }
+          item += t[i++];
+        }
+        item = "\x01" + item;  // marks a quoted string
+      } else {
+        while (i < t.size() && !std::isspace((unsigned char)t[i]) && t[i] != ',') item += t[i++];
+      }
+      v.items.push_back(item);
+    }
+    if (v.items.empty()) invalid_entry(src);
+    g[key] = v;
+  }
+  return g;
+}
+
+std::string nml_string(const NmlGroup& g, const std::string& key, const std::string& def) {
+  const NmlValue* v = find(g, key);
+  if (!v) return def;
+  std::string s = v->items[0];
+  if (!s.empty() && s[0] == '\x01') s = s.substr(1);
+  // Fortran character variables compare without trailing blanks.
+  while (!s.empty() && s.back() == ' ') s.pop_back();
+  return s;
+}
+
+long nml_int(const NmlGroup& g, const std::string& key, long def) {
+  const NmlValue* v = find(g, key);
+  if (!v) return def;
+  long x = 0;
+  if (v->items.size() != 1 || !parse_int(v->items[0], &x)) invalid_entry(v->line);
+  return x;
+}
+
+double nml_real(const NmlGroup& g, const std::string& key, double def) {
+  const NmlValue* v = find(g, key);
+  if (!v) return def;
+  double x = 0.0;
+  if (v->items.size() != 1 || !parse_real(v->items[0], &x)) invalid_entry(v->line);
+  return x;
+}
+
+bool nml_logical(const NmlGroup& g, const std::string& key, bool def) {
+  const NmlValue* v = find(g, key);
+  if (!v) return def;
+  std::string s = lower(strip(v->items[0]));
+  if (v->items.size() != 1 || s.empty()) invalid_entry(v->line);
+  if (s[0] == '.') s = s.substr(1);
+  if (!s.empty() && s[0] == 't') return true;
+  if (!s.empty() && s[0] == 'f') return false;
+  invalid_entry(v->line);
+}
+
+std::string format_g0(double x, int d) {
+  if (std::isnan(x)) return "NaN";
+  if (std::isinf(x)) return x > 0 ? "Infinity" : "-Infinity";
+  const std::string sign = std::signbit(x) ? "-" : "";
+  const double ax = std::fabs(x);
+  if (ax == 0.0) return sign + "0." + std::string(d - 1, '0');
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.*e", d - 1, ax);  // D.DDDDe+XX
+  const std::string s = buf;
+  const size_t epos = s.find('e');
+  std::string digits = s.substr(0, 1) + s.substr(2, epos - 2);
+  const int e10 = std::atoi(s.c_str() + epos + 1) + 1;  // ax = 0.DDDD * 10^e10
+  if (0 <= e10 && e10 <= d) {
+    if (e10 == 0) return sign + "0." + digits;
+    return sign + digits.substr(0, e10) + "." + digits.substr(e10);
+  }
+  return sign + "0." + digits + "E" + (e10 < 0 ? "-" : "+") + std::to_string(std::abs(e10));
+}
+
+std::vector<double> chebyshev_bins(int nbins, double xmin, double xmax) {
+  const double pi = std::acos(-1.0);
+  std::vector<double> b(nbins + 1);
+  for (int i = 1; i <= nbins + 1; ++i) b[i - 1] = xmin + (xmax - xmin) * (1.0 - std::cos(pi * (i - 1) / nbins)) / 2;
+  return b;
+}
+
+std::vector<double> linear_bins(int nbins, double xmin, double xmax) {
+  std::vector<double> b(nbins + 1);
+  for (int i = 1; i <= nbins + 1; ++i) b[i - 1] = xmin + (xmax - xmin) * (i - 1) / nbins;
+  return b;
+}
+
+Density density(const std::vector<double>& samples, const std::vector<double>& bins) {
+  Density d;
+  std::vector<double> h = recurgreen::histogram(samples, bins, &d.missing);
+  const double eps10 = std::numeric_limits<double>::epsilon() / 10.0;
+  for (double& v : h) v += eps10;
+  double npoints = 0.0;
+  for (double v : h) npoints += v;  // sum(histo), in order
+  d.rho.resize(h.size());
+  d.centre.resize(h.size());
+  for (size_t j = 0; j < h.size(); ++j) {
+    d.rho[j] = h[j] / (npoints * (bins[j + 1] - bins[j]));
+    d.centre[j] = ((0.0 + bins[j]) + bins[j + 1]) / 2;
+  }
+  return d;
+}
+
+std::vector<double> read_real_array(const std::string& path) {
+  std::vector<double> out;
+  std::ifstream f(path);
+  std::string line;
+  while (std::getline(f, line)) {
+    size_t a = 0;
+    while (a < line.size() && std::isspace((unsigned char)line[a])) ++a;
+    size_t b = a;
+    while (b < line.size() && !std::isspace((unsigned char)line[b]) && line[b] != ',' && line[b] != '/') ++b;
+    double v;
+    if (b > a && parse_real(line.substr(a, b - a), &v)) out.push_back(v);
+  }
+  return out;
+}
+
+std::string unique_filename(const std::string& base, const std::string& ext) {
+  for (long i = 1; i < 1000000000L; ++i) {
+    const std::string f = base + std::to_string(i) + ext;
+    if (!file_exists(f)) return f;
+  }
+  throw Stop("Too many files (nmax=1000000000), no valid filename !");
+}
+
+void create_directory(const std::string& dir) {
+  std::string cur;
+  for (size_t i = 0; i < dir.size(); ++i) {
+    cur += dir[i];
+    if (dir[i] == '/' || i + 1 == dir.size()) {
+      if (!cur.empty() && cur != "/" && ::mkdir(cur.c_str(), 0777) != 0 && errno != EEXIST)
+        throw Stop("Cannot create directory: " + cur);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// recurgreen: task tdistrib (src/main.f90:73-123)
+// ---------------------------------------------------------------------------
+namespace {
+
+void write_preamble(std::FILE* fp, const recurgreen::Waveguide& w, long nseed, long nbins, long nthreads,
+                    double tsec) {
+  std::fprintf(fp, "%%%% Computed on %s by %s\n", timestamp().c_str(), kProgram);
+  w.print_parameters(fp, "%%");
+  const double speed = nseed / tsec;
+  std::fprintf(fp, "%%%% Nseed=%ld, Nbins=%ld, Nthreads=%ld, Time=%s s, Speed=%s seed/s\n", nseed, nbins, nthreads,
+               format_g0(tsec, 6).c_str(), format_g0(speed, 6).c_str());
+}
+
+void task_tdistrib(const std::string& text, const std::string& root) {
+  const NmlGroup wg = read_namelist(text, "waveguide",
+                                    {"boundtype", "wol", "exfac", "dscat", "dabso", "aratio", "nxdiso", "nxfree",
+                                     "napera", "naperb", "ny"});
+  const NmlGroup td = read_namelist(text, "tdistrib", {"nseed", "nbins", "nthreads", "save_eigvals"});
+  recurgreen::Parameters p;
+  p.boundtype = nml_string(wg, "boundtype", "dirichlet");
+  p.wol = nml_real(wg, "wol", 0.0);
+  p.exfac = nml_real(wg, "exfac", 1.0);
+  p.dscat = nml_real(wg, "dscat", 0.0);
+  p.dabso = nml_real(wg, "dabso", 0.0);
+  p.aratio = nml_real(wg, "aratio", 1.0);
+  p.nxdiso = (int)nml_int(wg, "nxdiso", 0);
+  p.nxfree = (int)nml_int(wg, "nxfree", 0);
+  p.napera = nml_real(wg, "napera", 1.0);
+  p.naperb = nml_real(wg, "naperb", 1.0);
+  p.ny = (int)nml_int(wg, "ny", 0);
+  const long nseed = nml_int(td, "nseed", 0);
+  const long nbins = nml_int(td, "nbins", 0);
+  const long nthreads = nml_int(td, "nthreads", 1);
+  const bool save_eigvals = nml_logical(td, "save_eigvals", false);
+
+  recurgreen::Waveguide w(p);
+  const std::string info = strip(tag_info());
+  w.print_parameters(stdout, info);
+  std::printf("%sNseed=%ld, Nbins=%ld, Nthreads=%ld\n", tag_info().c_str(), nseed, nbins, nthreads);
+  if (nthreads < 1)
+    throw Stop("Invalid number of threads, received " + fmt_int(nthreads) + " expected >0, aborting...");
+  if (nseed < 0) throw Stop("Invalid number of seeds, received " + fmt_int(nseed) + " expected >=0, aborting...");
+  if (nbins < 1) throw Stop("Invalid number of bins, received " + fmt_int(nbins) + " expected >0, aborting...");
+
+  // The seed loop (src/main.f90:134-179) as one batched GPU launch.
+  std::vector<int32_t> seeds(nseed);
+  for (long k = 0; k < nseed; ++k) seeds[k] = (int32_t)(k + 1);
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<double> tallvals = nseed > 0 ? w.tdistrib_batch(seeds) : std::vector<double>();
+  const double tsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::printf("\n%sDone, computation time is %s s.\n", tag_info().c_str(), f0(tsec, 2).c_str());
+
+  // prepare_distrib (src/main.f90:223-251).
+  const std::vector<double> bins = chebyshev_bins((int)nbins);
+  const Density d = density(tallvals, bins);
+  if (d.missing != 0.0) {
+    std::printf("%sSome transmission eigenvalues are out of the bounds [%s, %s].\n%sThere are %s missing "
+                "eigenvalues in the histogram, continuing anyway...\n",
+                tag_warn().c_str(), f0(bins.front(), 6).c_str(), f0(bins.back(), 6).c_str(), tag_warn().c_str(),
+                f0(d.missing, 1).c_str());
+  }
+
+  // save_distrib / save_raw_eigvals (src/main.f90:257-328).
+  const std::string dir = w.generate_directory(root) + "distrib/";
+  create_directory(dir);
+  const std::string fname = unique_filename(dir + "result_", ".distrib.csv");
+  std::FILE* fp = std::fopen(fname.c_str(), "w");
+  if (!fp) throw Stop("Cannot open file: " + fname);
+  write_preamble(fp, w, nseed, nbins, nthreads, tsec);
+  std::fprintf(fp, "tm, rho\n");
+  write_rows(fp, d);
+  std::fclose(fp);
+  std::printf("%sResult written in file: %s\n", tag_info().c_str(), fname.c_str());
+  if (save_eigvals) {
+    const std::string ename = unique_filename(dir + "result_", ".eigvals.csv");
+    std::FILE* fe = std::fopen(ename.c_str(), "w");
+    if (!fe) throw Stop("Cannot open file: " + ename);
+    write_preamble(fe, w, nseed, nbins, nthreads, tsec);
+    std::fprintf(fe, "%%%% Transmission eigenvalues (%zu values)\n", tallvals.size());
+    for (double v : tallvals) std::fprintf(fe, "%s\n", format_g0(v).c_str());
+    std::fclose(fe);
+    std::printf("%sEigenvalues saved in file: %s\n", tag_info().c_str(), ename.c_str());
+  }
+}
+
+// execute_file (src/main.f90:41-65).
+void execute_file(const std::string& text, const std::string& root) {
+  const NmlGroup s = read_namelist(text, "settings", {"task"});
+  const std::string task = nml_string(s, "task", "");
+  if (task == "tdistrib") {
+    task_tdistrib(text, root);
+  } else if (task == "wavefunction" || task == "tprofile" || task == "tprofile_group" || task == "tpattern") {
+    throw Stop("Task '" + task + "' is not part of this GPU build, which runs the tdistrib task, aborting...");
+  } else {
+    throw Stop("Unknown task '" + task + "', aborting...");
+  }
+}
+
+int stop_exit(const std::string& msg) {
+  std::fprintf(stderr, "%s%s\n", tag_error().c_str(), msg.c_str());
+  std::fprintf(stderr, "STOP %s\n", kStopMessage);
+  return 1;
+}
+
+}  // namespace
+
+int recurgreen_main(int argc, char** argv) {
+  std::printf("====== This is %s ======\n", kProgram);
+  std::fflush(stdout);
+  std::string root = "out";
+  std::vector<std::string> files;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    if (a == "--outdir" && i + 1 < argc) {
+      root = argv[++i];
+    } else {
+      files.push_back(a);
+    }
+  }
+  if (files.empty()) std::fprintf(stderr, "%sNo settings file provided, doing nothing...\n", tag_error().c_str());
+  int rc = 0;
+  for (const std::string& f : files) {
+    if (!file_exists(f)) {
+      std::fprintf(stderr, "%sFile not found: %s\n", tag_error().c_str(), f.c_str());
+      rc = 1;
+      continue;
+    }
+    std::ifstream probe(f);
+    if (!probe) {
+      std::fprintf(stderr, "%sCannot open file: %s\n", tag_error().c_str(), f.c_str());
+      rc = 1;
+      continue;
+    }
+    std::printf("%sReading file: %s\n", tag_info().c_str(), f.c_str());
+    std::fflush(stdout);
+    try {
+      execute_file(read_file(f), root);
+    } catch (const Stop& e) {
+      std::fflush(stdout);
+      return stop_exit(e.what());
+    } catch (const recurgreen::Error& e) {
+      std::fflush(stdout);
+      return stop_exit(e.what());
+    }
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// plothisto (src/plot_histogram.f90)
+// ---------------------------------------------------------------------------
+int plothisto_main(int argc, char** argv) {
+  std::printf("====== This is PlotHisto (from %s) ======\n", kProgram);
+  std::fflush(stdout);
+  try {
+    if (argc != 3) {
+      std::printf("%sUsage: $ ./plothisto plothisto_settings.nml path/to/samples.csv\n", tag_info().c_str());
+      throw Stop("Two files expected, doing nothing...");
+    }
+    const std::string cfg = argv[1], data = argv[2];
+    if (!file_exists(cfg)) throw Stop("File not found: " + cfg);
+    if (!file_exists(data)) throw Stop("File not found: " + data);
+    const NmlGroup s = read_namelist(read_file(cfg), "settings", {"bintype", "nbins", "xmin", "xmax"});
+    const std::string bintype = nml_string(s, "bintype", "chebyshev");
+    const long nbins = nml_int(s, "nbins", 0);
+    const double xmin = nml_real(s, "xmin", 0.0), xmax = nml_real(s, "xmax", 1.0);
+    const std::vector<double> samples = read_real_array(data);
+    std::printf("%sFound %zu samples in the data file...\n", tag_info().c_str(), samples.size());
+    if (nbins < 1)
+      throw Stop("Invalid number of bins (nbins=" + fmt_int(nbins) + " must be positive), aborting...");
+    if (!(xmax > xmin)) throw Stop("Invalid binning range, aborting...");
+    std::vector<double> bins;
+    if (bintype == "linear") {
+      bins = linear_bins((int)nbins, xmin, xmax);
+    } else if (bintype == "chebyshev") {
+      bins = chebyshev_bins((int)nbins, xmin, xmax);
+    } else {
+      throw Stop("Unknown binning type '" + bintype + "', aborting...");
+    }
+    const Density d = density(samples, bins);
+    if (d.missing != 0.0) {
+      std::printf("%sSome samples are out of the bounds [%s, %s].\n%sThere are %s missing samples in the histogram "
+                  "(%s%%), continuing anyway...\n",
+                  tag_warn().c_str(), f0(bins.front(), 6).c_str(), f0(bins.back(), 6).c_str(), tag_warn().c_str(),
+                  f0(d.missing, 0).c_str(), f0(100.0 * d.missing / samples.size(), 2).c_str());
+    }
+    // save_histo: replot_<i>.distrib.csv beside the data file, with its preamble.
+    const size_t slash = data.rfind('/');
+    const std::string dir = slash == std::string::npos ? "" : data.substr(0, slash + 1);
+    const std::string out = unique_filename(dir + "replot_", ".distrib.csv");
+    std::FILE* fp = std::fopen(out.c_str(), "w");
+    if (!fp) throw Stop("Cannot open file: " + out);
+    std::ifstream in(data);
+    std::string line;
+    while (std::getline(in, line)) {  // copy_preamble (src/base_utils.f90:856-872)
+      if (line.empty() || (line[0] != '%' && line[0] != '#')) break;
+      if (line.size() > 300) line.resize(300);
+      while (!line.empty() && (line.back() == ' ' || line.back() == '\r')) line.pop_back();
+      std::fprintf(fp, "%s\n", line.c_str());
+    }
+    std::fprintf(fp, "tm, rho\n");
+    write_rows(fp, d);
+    std::fclose(fp);
+    std::printf("%sReplot written in file: %s\n", tag_info().c_str(), out.c_str());
+  } catch (const Stop& e) {
+    std::fflush(stdout);
+    return stop_exit(e.what());
+  } catch (const recurgreen::Error& e) {
+    std::fflush(stdout);
+    return stop_exit(e.what());
+  }
+  return 0;
+}
+
+}  // namespace rgdriver

@@ -121,8 +121,27 @@ def fortran_g0(x: float, d: int = 16) -> str:
 
 
 def fortran_f(x: float, d: int = 6) -> str:
-    """Fortran F0.d output."""
-    return f"{x:.{d}f}"
+    """Fortran F0.d output as gfortran writes it: with no field width there is
+    no leading zero below one (0.2 -> ".200000"); F0.0 keeps the point."""
+    t = f"{x:.{d}f}"
+    if t.startswith("0."):
+        t = t[1:]
+    elif t.startswith("-0."):
+        t = "-" + t[2:]
+    return t + "." if d == 0 else t
+
+
+def generate_directory(w: Waveguide, root: str = "out") -> str:
+    """generate_directory (src/waveguide.f90:1046-1067):
+    root/dscat_X/dabso_Y/wol_Z/boundtype/ with F0.6 values, trailing zeros
+    removed (a zero is put before the point of values below one)."""
+    p = w.get_parameters()
+
+    def folder(stem, v):
+        return (stem + ("0" if v < 1.0 else "") + fortran_f(v)).rstrip("0 ")
+
+    return os.path.join(root, folder("dscat_", p["dscat"]), folder("dabso_", p["dabso"]), folder("wol_", p["wol"]),
+                        str(p["boundtype"]).strip()) + os.sep
 
 
 # ---------------------------------------------------------------------------
@@ -172,14 +191,15 @@ def _preamble(w: Waveguide, nseed: int, nbins: int, nthreads: int, tsec: float, 
     now = datetime.datetime.now().astimezone()
     speed = nseed / tsec if tsec > 0 else float("inf")
     return [
-        f"{prefix} Computed on {now:%Y-%m-%d at %H:%M:%S %Z} by {PROGRAM}",
+        f"{prefix} Computed on {now:%Y-%m-%d at %H:%M:%S %z} by {PROGRAM}",
         f"{prefix} Waveguide 2D with boundtype='{p['boundtype']}', W/lambda={fortran_f(p['wol'])}, "
         f"exfac={fortran_f(p['exfac'])}, Nmode={w.nmu}, Nprop={w.nprop}",
         f"{prefix} Filtering: NAper_a={fortran_f(p['napera'])} (Nmode_a={w.jmax - w.jmin + 1}), "
         f"NAper_b={fortran_f(p['naperb'])} (Nmode_b={w.imax - w.imin + 1}), Neigv={w.neigv}",
         f"{prefix} Medium: L/lscat={fortran_f(p['dscat'])}, L/labso={fortran_f(p['dabso'])}, "
         f"Nx_diso={p['nxdiso']}, Nx_free={p['nxfree']}, aratio=L/W={fortran_f(p['aratio'])}",
-        f"{prefix} Nseed={nseed}, Nbins={nbins}, Nthreads={nthreads}, Time={tsec:.6g} s, Speed={speed:.6g} seed/s",
+        f"{prefix} Nseed={nseed}, Nbins={nbins}, Nthreads={nthreads}, Time={fortran_g0(tsec, 6)} s, "
+        f"Speed={fortran_g0(speed, 6)} seed/s",
     ]
 
 
@@ -230,13 +250,14 @@ def task_tdistrib(settings: dict, outdir: str = "out") -> dict:
     tallvals = w.tdistrib_batch(np.arange(1, nseed + 1, dtype=np.int32))
     tsec = time.perf_counter() - t0
     rho, missing = prepare_distrib(tallvals, nbins)
-    os.makedirs(os.path.join(outdir, "distrib"), exist_ok=True)
-    pre = _preamble(w, nseed, nbins, 1, tsec)
-    dpath = unique_filename(os.path.join(outdir, "distrib", "result_"), ".distrib.csv")
+    ddir = os.path.join(generate_directory(w, outdir), "distrib")
+    os.makedirs(ddir, exist_ok=True)
+    pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec)
+    dpath = unique_filename(os.path.join(ddir, "result_"), ".distrib.csv")
     save_distrib(dpath, rho, pre)
     res = {"distrib": dpath, "tallvals": tallvals, "rho": rho, "missing": missing, "time": tsec}
     if td.get("save_eigvals", False):
-        epath = unique_filename(os.path.join(outdir, "distrib", "result_"), ".eigvals.csv")
+        epath = unique_filename(os.path.join(ddir, "result_"), ".eigvals.csv")
         save_raw_eigvals(epath, tallvals, pre)
         res["eigvals"] = epath
     return res
