@@ -518,11 +518,14 @@ int size_bucket(int n) {
 }
 
 // Times one configuration on the proxy (ms); large values mean "unusable".
+// seg_end > 0 stops the (blocked-kernel) sweep after that many slices, before
+// the Fisher-Lee and eigenvalue stage.
 double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const int32_t* d_seeds, double* d_teig,
-                      int32_t* d_status, const TuneChoice& tc, cudaStream_t s) {
+                      int32_t* d_status, const TuneChoice& tc, int seg_end, cudaStream_t s) {
   rg::SweepArgs a = make_args(w, rg::kModeEig);
   a.wgs = d_proxy;
   a.nreal = n;
+  a.n_end = seg_end;
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
@@ -582,11 +585,16 @@ TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
     g_tune_cache[key] = cands[0];
     return cands[0];
   }
-  // Proxy: the same waveguide cut to 16 slices (all disordered).
+  // Proxy: the same waveguide cut to 16 slices (all disordered).  When only
+  // blocked-kernel cluster sizes compete (M > 64), the proxy stops before
+  // the eigenvalue stage: at the sizes that reach this kernel that stage is a
+  // negligible part of a real guide but would dominate 16 slices.
   rg::WgDesc pd = w->h_desc;
-  pd.nx = std::min(pd.nx, 16);
+  const bool blocked_only = w->nmu > rg::kMaxModesSmem;
+  pd.nx = std::min(pd.nx, 16) + (blocked_only ? 1 : 0);
   pd.nxfree = 0;
   pd.nxdiso = pd.nx;
+  const int seg_end = blocked_only ? pd.nx - 1 : 0;
   const int np = std::min(n, 4 * w->sm_count);
   char* buf = nullptr;
   const size_t b_desc = align256(sizeof pd), b_seed = align256(sizeof(int32_t) * np);
@@ -606,7 +614,7 @@ TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   TuneChoice best = cands[0];
   double tbest = 1e30;
   for (const TuneChoice& c : cands) {
-    const double t = time_candidate(w, d_pd, np, d_seeds, d_teig, d_status, c, s);
+    const double t = time_candidate(w, d_pd, np, d_seeds, d_teig, d_status, c, seg_end, s);
     if (t < tbest) {
       tbest = t;
       best = c;
