@@ -113,33 +113,73 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
       const int id = (refl ? nx - 1 - n : n) - wd.nxfree;
       const bool dis = (id >= 0 && id < wd.nxdiso);
       if (dis) {
-        // 1. This slice's potential row and its projection coefficients.
-        if (draw) {
-          for (int iy = tid; iy < ny; iy += NT) {
-            Xoshiro st{gen[4 * iy], gen[4 * iy + 1], gen[4 * iy + 2], gen[4 * iy + 3]};
-            urow[iy] = scaled_normal(wd.stdu, st);
-            gen[4 * iy + 0] = st.s0;
-            gen[4 * iy + 1] = st.s1;
-            gen[4 * iy + 2] = st.s2;
-            gen[4 * iy + 3] = st.s3;
+        // 1. This slice's potential row and its projection coefficients
+        //    cc[d] = sum_j costab[j][d] U_j.  The transverse grid is symmetric
+        //    (y_{ny-1-j} = 1 - y_j) and cos(pi d (1 - y)) = (-1)^d cos(pi d y),
+        //    so the points pair up: urow[j] = U_j + U_j', urow[j'] = U_j - U_j'
+        //    (j < ny/2, j' = ny-1-j), and even d sums costab[j][d] urow[j],
+        //    odd d sums costab[j][d] urow[j'], over half the points.
+        const int h = ny >> 1;
+        for (int j = tid; j < h + (ny & 1); j += NT) {
+          const int jp = ny - 1 - j;
+          double u0 = 0.0, u1 = 0.0;
+          if (draw) {
+            Xoshiro st{gen[4 * j], gen[4 * j + 1], gen[4 * j + 2], gen[4 * j + 3]};
+            u0 = scaled_normal(wd.stdu, st);
+            gen[4 * j + 0] = st.s0;
+            gen[4 * j + 1] = st.s1;
+            gen[4 * j + 2] = st.s2;
+            gen[4 * j + 3] = st.s3;
+            if (jp != j) {
+              Xoshiro sq{gen[4 * jp], gen[4 * jp + 1], gen[4 * jp + 2], gen[4 * jp + 3]};
+              u1 = scaled_normal(wd.stdu, sq);
+              gen[4 * jp + 0] = sq.s0;
+              gen[4 * jp + 1] = sq.s1;
+              gen[4 * jp + 2] = sq.s2;
+              gen[4 * jp + 3] = sq.s3;
+            }
+          } else {
+            u0 = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+            u1 = U[(int64_t)id * a.pot_xstride + (int64_t)jp * a.pot_ystride];
           }
-        } else {
-          for (int j = tid; j < ny; j += NT) urow[j] = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+          if (jp == j) {
+            urow[j] = u0;  // middle point of an odd grid
+          } else {
+            urow[j] = u0 + u1;
+            urow[jp] = u0 - u1;
+          }
         }
         __syncthreads();
+        // Coefficients d < NT/2 take one thread each in the first half of the
+        // CTA (one warp per SMSP); d = NT/2 = 2*MCAP, present when M = MCAP,
+        // takes one warp of the second half with a shuffle reduction.
         const int nd = 2 * M + 1;
-        for (int d = tid; d < nd; d += NT) {
-          const double* ct = wd.costab + d;
-          double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-          int j = 0;
-          for (; j + 4 <= ny; j += 4) {
-            s0 = fma(ct[(int64_t)(j + 0) * nd], urow[j + 0], s0);
-            s1 = fma(ct[(int64_t)(j + 1) * nd], urow[j + 1], s1);
-            s2 = fma(ct[(int64_t)(j + 2) * nd], urow[j + 2], s2);
-            s3 = fma(ct[(int64_t)(j + 3) * nd], urow[j + 3], s3);
+        if (tid < NT / 2) {
+          for (int d = tid; d < nd && d < NT / 2; d += NT / 2) {
+            const double* ct = wd.costab + d;
+            const double* up = (d & 1) ? urow + (ny - 1) : urow;
+            const int us = (d & 1) ? -1 : 1;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int j = 0;
+            for (; j + 4 <= h; j += 4) {
+              s0 = fma(ct[(int64_t)(j + 0) * nd], up[us * (j + 0)], s0);
+              s1 = fma(ct[(int64_t)(j + 1) * nd], up[us * (j + 1)], s1);
+              s2 = fma(ct[(int64_t)(j + 2) * nd], up[us * (j + 2)], s2);
+              s3 = fma(ct[(int64_t)(j + 3) * nd], up[us * (j + 3)], s3);
+            }
+            for (; j < h; ++j) s0 = fma(ct[(int64_t)j * nd], up[us * j], s0);
+            if (ny & 1) s1 = fma(ct[(int64_t)h * nd], urow[h], s1);
+            cc[d] = (s0 + s1) + (s2 + s3);
           }
-          for (; j < ny; ++j) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
-          cc[d] = (s0 + s1) + (s2 + s3);
+        } else if (warp == NW / 2 && nd > NT / 2) {
+          const int d = NT / 2;  // even
+          const double* ct = wd.costab + d;
+          double s0 = 0.0;
+          for (int j = lane; j < h; j += 32) s0 = fma(ct[(int64_t)j * nd], urow[j], s0);
+          if ((ny & 1) && lane == 0) s0 = fma(ct[(int64_t)h * nd], urow[h], s0);
+#pragma unroll
+          for (int off = 16; off; off >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, off);
+          if (lane == 0) cc[d] = s0;
         }
         __syncthreads();
       }
@@ -148,9 +188,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
       //    element is read and written by one thread), and R = B Gs1.
       const double2* adiag = (n == 0 || n == nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
       const double rsign = (n == 1) ? 1.0 : -1.0;
+      const int arot = (tid + NT - 32 * (n % NW)) % NT;  // the partial chunk rotates over the warps
 #pragma unroll
       for (int s = 0; s < SMAX; ++s) {
-        const int e = tid + NT * s;
+        const int e = arot + NT * s;
         if (e < T) {
           const int i = tri[e] >> 16, j = tri[e] & 0xffff;
           double2 x = (i == j) ? adiag[i] : make_double2(0.0, 0.0);
@@ -173,9 +214,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
       for (int c = tid; c < M; c += NT) used[c] = 0;
       __syncthreads();
 
-      // 3. Symmetric Gauss-Jordan, three barriers per step.
+      // 3. Symmetric Gauss-Jordan, three barriers per step.  Phase A runs on
+      //    warp k % NW and the partial chunk of the triangle update on warp
+      //    (k + 2) % NW, so their extra FP64 work rotates over the SMSPs.
       for (int k = 0; k < M; ++k) {
-        if (warp == 0) {
+        if (warp == k % NW) {
           // A. pivot: the largest unswept diagonal element
           unsigned long long best = 0ULL;
           int bi = 0x7fffffff;
@@ -265,9 +308,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
         //      (i, j), i, j != p:  W - g_i rowW[j]
         //      (p, j):             rowW[j] - 0 * rowW[j]
         //      (i, p), i < p:      0 - g_i d
+        const int crot = (tid + NT - 32 * ((k + 2) % NW)) % NT;
 #pragma unroll
         for (int s = 0; s < SMAX; ++s) {
-          const int e = tid + NT * s;
+          const int e = crot + NT * s;
           if (e < T) {
             const int i = tri[e] >> 16, j = tri[e] & 0xffff;
             const double2 rj = rowW[j];

@@ -484,22 +484,25 @@ int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
 
 // ---------------------------------------------------------------------------
 // Autotuner.  For a waveguide shape (M, ny) and a batch size, the candidate
-// launch configurations -- for M <= 64 the symmetric kernel (Dirichlet),
-// the pivoted shared-memory kernel or the blocked kernel, and above 64 modes
-// the blocked kernel's cluster size (CTAs per realization) -- are timed once on a short proxy guide (the same modes and grid, 16
+// launch configurations -- the blocked kernel's cluster size (CTAs per
+// realization), above 64 modes -- are timed once on a short proxy guide (the same modes and grid, 16
 // slices, the same number of realizations) and the fastest is cached for the
 // process.  RG_AUTOTUNE=0 disables it (the built-in heuristics decide).
+// Only choices that leave every realization's result bit for bit the same
+// are tuned: the cluster size changes which CTA computes an element, not its
+// arithmetic.  The kernel itself (symmetric for Dirichlet guides of up to 64
+// modes, pivoted shared-memory for periodic ones, blocked above 64 modes) is
+// fixed, so a realization gives the same bits in a batch of any size and in
+// a single call.
 // ---------------------------------------------------------------------------
 struct TuneChoice {
-  int force_large = 0;
   int force_cluster = 0;
-  int general = 0;  // 1: the pivoted kernel even where the symmetric one applies
 };
 
 struct TuneKey {
-  int M, ny, bucket, sms, sym;
+  int M, ny, bucket, sms;
   bool operator<(const TuneKey& o) const {
-    return std::tie(M, ny, bucket, sms, sym) < std::tie(o.M, o.ny, o.bucket, o.sms, o.sym);
+    return std::tie(M, ny, bucket, sms) < std::tie(o.M, o.ny, o.bucket, o.sms);
   }
 };
 
@@ -529,9 +532,7 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
-  a.force_large = tc.force_large;
   a.force_cluster = tc.force_cluster;
-  a.symmetric = a.symmetric && !tc.general;
   int grid = 0;
   int64_t stride = 0;
   if (rg::sweep_plan(a, w->sm_count, &grid, &stride) != RG_OK) return 1e30;
@@ -564,37 +565,29 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
 
 TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   TuneChoice def;
-  if (!autotune_enabled() || n <= 0) return def;
-  const int sym = make_args(w, rg::kModeEig).symmetric;
-  const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count, sym};
+  if (!autotune_enabled() || n <= 0 || w->nmu <= rg::kMaxModesSmem) return def;
+  const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count};
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) return it->second;
   }
   std::vector<TuneChoice> cands;
-  if (w->nmu <= rg::kMaxModesSmem) {
-    cands.push_back(TuneChoice{0, 0, 0});
-    if (sym) cands.push_back(TuneChoice{0, 0, 1});
-    if (w->nmu > 32) cands.push_back(TuneChoice{1, 1, 0});
-  } else {
-    for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{1, c, 0});
-  }
+  for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{c});
   if (cands.size() == 1) {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     g_tune_cache[key] = cands[0];
     return cands[0];
   }
-  // Proxy: the same waveguide cut to 16 slices (all disordered).  When only
-  // blocked-kernel cluster sizes compete (M > 64), the proxy stops before
-  // the eigenvalue stage: at the sizes that reach this kernel that stage is a
-  // negligible part of a real guide but would dominate 16 slices.
+  // Proxy: the same waveguide cut to 16 slices (all disordered), stopped
+  // before the eigenvalue stage: at the sizes that reach the blocked kernel
+  // that stage is a negligible part of a real guide but would dominate 16
+  // slices.
   rg::WgDesc pd = w->h_desc;
-  const bool blocked_only = w->nmu > rg::kMaxModesSmem;
-  pd.nx = std::min(pd.nx, 16) + (blocked_only ? 1 : 0);
+  pd.nx = std::min(pd.nx, 16) + 1;
   pd.nxfree = 0;
   pd.nxdiso = pd.nx;
-  const int seg_end = blocked_only ? pd.nx - 1 : 0;
+  const int seg_end = pd.nx - 1;
   const int np = std::min(n, 4 * w->sm_count);
   char* buf = nullptr;
   const size_t b_desc = align256(sizeof pd), b_seed = align256(sizeof(int32_t) * np);
@@ -641,9 +634,7 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
-  a.force_large = tc.force_large;
   a.force_cluster = tc.force_cluster;
-  a.symmetric = a.symmetric && !tc.general;
   int grid = 0, rc;
   if ((rc = place_workspace(w, a, 0, &grid))) return rc;
   int64_t tau_bits = 0;

@@ -289,11 +289,14 @@ def test_batch_graph_replay_and_autotune(monkeypatch):
 
 
 def test_large_autotuned_cluster_matches():
+    """The cluster size only moves work between CTAs: a realization gives the
+    same bits whatever cluster the autotuner or the heuristic picks."""
     kw = dict(LARGE["m128"], nxdiso=6)
     g = rg.Waveguide(**kw)
     seeds = np.arange(1, 9, dtype=np.int32)
     b = g.tdistrib_batch(seeds)  # autotuned cluster size
+    assert g.last_batch_info()["kernel"] == "blocked"
     for k, s in enumerate(seeds[:3]):
         one = np.zeros(s * g.neigv)
         g.compute_tdistrib(int(s), one)  # single realization: cluster of 8
-        assert np.max(np.abs(b[k * g.neigv:(k + 1) * g.neigv] - one[(s - 1) * g.neigv:])) <= 1e-12
+        np.testing.assert_array_equal(b[k * g.neigv:(k + 1) * g.neigv], one[(s - 1) * g.neigv:])
