@@ -186,6 +186,7 @@ int rg_last_sweep_time(rg_waveguide* wg, float* ms);
 #define RG_KERNEL_PIVOTED 0   /* shared-memory Gauss-Jordan with implicit partial pivoting */
 #define RG_KERNEL_SYMMETRIC 1 /* symmetric sweep (Dirichlet), pivoted re-run of flagged items */
 #define RG_KERNEL_BLOCKED 2   /* blocked global-memory kernel, `cluster` CTAs per realization */
+#define RG_KERNEL_BLOCKED_SYMMETRIC 3 /* blocked symmetric sweep (Dirichlet), blocked pivoted re-run */
 typedef struct rg_batch_info {
   int kernel;  /* RG_KERNEL_* */
   int grid;    /* CTAs of the launch */

@@ -29,7 +29,7 @@ EXPORTS = (
     "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi", "rg_sweep_segment",
     "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info",
 )
-KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked"}
+KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
 
 
 class RecurGreenError(RuntimeError):

@@ -78,9 +78,9 @@ struct SweepArgs {
   double2* state_dump;        // [nreal][n_end-n_begin][2][M][M] (Gss, Gs1) after every slice, optional
   double2* state_out;         // [nreal][2][M][M] state after slice n_end-1, optional
   int force_large;            // 1: use the blocked global-memory kernel even for max_M <= 64 (autotuner)
-  // Symmetric sweep (Dirichlet items, max_M <= kMaxModesSmem): the symmetric
-  // kernel runs every item and appends those it cannot pivot stably to
-  // flag_list; the pivoted kernel then re-runs that list.
+  // Symmetric sweep (Dirichlet items): the symmetric kernel (shared-memory
+  // or blocked, by max_M) runs every item and appends those it cannot pivot
+  // stably to flag_list; the pivoted kernel of the same class re-runs them.
   int symmetric;              // 1: symmetric kernel first (needs flag_list)
   int32_t* flag_list;         // [nreal] flagged item indices
   double sym_tau;             // smallest accepted |diagonal pivot| / max |unswept entry of its row|
@@ -126,6 +126,10 @@ int launch_sweep_sym(const SweepArgs& a, cudaStream_t stream, int grid);
 // The large-mode kernel behind sweep_plan/launch_sweep for max_M > kMaxModesSmem (rg_sweep_large.cu).
 int sweep_large_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
 int launch_sweep_large(const SweepArgs& a, cudaStream_t stream, int grid);
+// Its symmetric counterpart for Dirichlet guides (rg_sweep_large_sym.cu);
+// launch_sweep re-runs the items it flags with the pivoted one.
+int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride);
+int launch_sweep_large_sym(const SweepArgs& a, cudaStream_t stream, int grid);
 // Adjoint (rg_adjoint.cu): dL/dU rows of n realizations from their slice-matrix adjoints.
 int launch_grad_rows(const WgDesc* d_desc, int M, const double2* xbar, int n, double* grad, int64_t gstride,
                      cudaStream_t s);

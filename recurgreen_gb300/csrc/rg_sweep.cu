@@ -479,8 +479,28 @@ int launch_potential(const PotArgs& a, cudaStream_t stream) {
 // run on the same grid and per-CTA workspace (the larger of their plans).
 int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
   if (a.force_large || a.max_M > kMaxModesSmem) {
-    a.symmetric = 0;
-    return sweep_large_plan(a, sm_count, grid, work_stride);
+    // The symmetric blocked kernel, unless segment states are asked for (the
+    // adjoint's recomputation forces the pivoted one); the pivoted re-run
+    // uses the same cluster size, grid and workspace.
+    if (!a.symmetric || a.force_large || a.state_in || a.state_dump || a.state_out) {
+      a.symmetric = 0;
+      return sweep_large_plan(a, sm_count, grid, work_stride);
+    }
+    int rc = sweep_large_sym_plan(a, sm_count, grid, work_stride);
+    if (rc) return rc;
+    SweepArgs b = a;
+    b.symmetric = 0;
+    b.force_cluster = a.cluster;
+    int g2 = 0;
+    int64_t s2 = 0;
+    if ((rc = sweep_large_plan(b, sm_count, &g2, &s2))) return rc;
+    if (b.cluster != a.cluster) {  // the pivoted kernel cannot run clusters of this size
+      a.symmetric = 0;
+      return sweep_large_plan(a, sm_count, grid, work_stride);
+    }
+    *grid = std::max(*grid, g2);
+    *work_stride = std::max(*work_stride, s2);
+    return RG_OK;
   }
   int rc;
   if (a.max_M <= 16) rc = plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
@@ -499,12 +519,16 @@ int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
 
 int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  if (a.force_large || a.max_M > kMaxModesSmem) return launch_sweep_large(a, stream, grid);
+  const bool blocked = a.force_large || a.max_M > kMaxModesSmem;
+  if (!a.symmetric) {
+    if (blocked) return launch_sweep_large(a, stream, grid);
+  } else if (!a.flag_list) {
+    return fail(RG_ERR_INVALID_ARG, "symmetric sweep: no flag list");
+  }
   const SweepArgs* p = &a;
   SweepArgs rerun;
   if (a.symmetric) {
-    if (!a.flag_list) return fail(RG_ERR_INVALID_ARG, "symmetric sweep: no flag list");
-    int rc = launch_sweep_sym(a, stream, grid);
+    int rc = blocked ? launch_sweep_large_sym(a, stream, grid) : launch_sweep_sym(a, stream, grid);
     if (rc) return rc;
     // The pivoted kernel takes the flagged items: queue length in counter 1,
     // its own queue position in counter 2.
@@ -514,6 +538,7 @@ int launch_sweep(const SweepArgs& a, cudaStream_t stream, int grid) {
     rerun.count_ptr = a.work_counter + 1;
     rerun.work_counter = a.work_counter + 2;
     p = &rerun;
+    if (blocked) return launch_sweep_large(rerun, stream, grid);
   }
   if (a.max_M <= 16) return launch_t<16, 64, 8>(*p, stream, grid);
   if (a.max_M <= 32) return launch_t<32, 128, 4>(*p, stream, grid);

@@ -90,17 +90,19 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
 
   for (;;) {
     if (rank == 0 && tid == 0) {
-      s_r = atomicAdd(a.work_counter, 1);
-      if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
+      const int q = atomicAdd(a.work_counter, 1);
+      const int nq = a.count_ptr ? *a.count_ptr : a.nreal;
+      s_r = q < nq ? (a.item_idx ? a.item_idx[q] : q) : -1;
+      if (s_r >= 0) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
     }
     cluster.sync();
     if (rank != 0 && tid == 0) {
       s_r = *cluster.map_shared_rank(&s_r, 0);
-      if (s_r < a.nreal) wd = *cluster.map_shared_rank(&wd, 0);
+      if (s_r >= 0) wd = *cluster.map_shared_rank(&wd, 0);
     }
     cluster.sync();  // rank 0's shared memory has been read before any CTA can leave the loop
-    const int r = s_r;
-    if (r >= a.nreal) break;
+    const int r = s_r;  // item index (queue position mapped through item_idx)
+    if (r < 0) break;
     const int M = wd.M, ny = wd.ny;
     const int64_t mm = (int64_t)M * M;
     double2* ws = a.work + (int64_t)(blockIdx.x / C) * a.work_stride;

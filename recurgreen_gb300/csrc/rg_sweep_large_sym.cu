@@ -1,0 +1,669 @@
+// Symmetric blocked sweep for Dirichlet guides of more than 64 modes.
+//
+// The slice matrix X_n = A_n - V_n - B Gss B of a Dirichlet guide is complex
+// symmetric, so its inverse is formed by a symmetric Gauss-Jordan sweep on
+// the upper triangle (the shared-memory version and its sign rule are in
+// rg_sweep_sym.cu), here blocked for matrices that live in global memory
+// (L2-resident when the batch allows):
+//
+//   for each panel of NB diagonal pivots
+//     for each step k of the panel (left-looking)
+//       p_k = the unswept index with the largest current diagonal |dg_i|,
+//       x   = column p_k at the panel start (upper triangle plus sign rule),
+//             plus the panel's earlier steps: x += U z, z = (I - L)^-1 x[p],
+//       u_k = -x d (u_k[p_k] = d - 1), d = 1 / x[p_k],
+//       dg_i += u_k[i] x[i] for the unswept i;
+//     every other column j of [W | R] gets x += U z with z = (I - L)^-1 x[p]
+//       (a rank-NB update, rows i <= j only for W: half the work),
+//     pivot column p_k becomes u_k + e_{p_k} with the later steps applied.
+//
+// A slice costs 12 M^3 + O(M^2) FP64 flops instead of the pivoted blocked
+// kernel's 16 M^3 (src/waveguide.f90:426-440: zgetrf+zgetri and a matmul).
+// W and R stay in natural order, so there is no permutation bookkeeping.
+// The z of a W column comes from the panel's raw pivot columns, which each
+// CTA keeps in its own staging area: no column reads another column's
+// storage during the update, so one cluster barrier per panel suffices.
+//
+// A diagonal pivot below sym_tau times the largest unswept entry of its
+// column flags the realization (kStatusNeedPivot, appended to flag_list);
+// launch_sweep then re-runs the flagged ones with the pivoted blocked kernel.
+// Periodic items (Hermitian, not symmetric) are flagged at once.  Segment
+// mode supports a stop after n_end slices (no Fisher-Lee stage), not states.
+#include <cooperative_groups.h>
+
+#include "rg_device.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rg {
+namespace {
+
+constexpr int kSymNT = 256;
+constexpr int kSymNB = 8;
+constexpr int kSymMaxCluster = 8;
+constexpr int kSymMaxRowSplit = 8;
+
+// The pivot column (panel phase) and the chunk's z values (update phase)
+// share one region: they are never live at the same time.
+struct LargeSymSmem {
+  __host__ __device__ static size_t shared_region(int M) {
+    const size_t z = (size_t)(kSymNT / 2) * kSymNB;
+    return (size_t)M > z ? (size_t)M : z;
+  }
+  static size_t bytes(int M) {
+    return sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
+           sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
+  }
+};
+
+// Workspace of one cluster, in double2 units: W, R, t (M x M each), the
+// generator states (ny x 4 uint64), the paired potential row (ny doubles)
+// and each CTA's raw pivot columns (kSymMaxCluster x NB x M).
+inline int64_t large_sym_stride(int M, int ny) {
+  const int64_t mm = (int64_t)M * M;
+  const int64_t urow = ((int64_t)ny + 1) / 2;
+  return ((3 * mm + 2 * (int64_t)ny + urow + (int64_t)kSymMaxCluster * kSymNB * M) + 15) & ~(int64_t)15;
+}
+
+__device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+
+__global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a) {
+  constexpr int NT = kSymNT, NB = kSymNB, NW = NT / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int MX = a.max_M;
+  extern __shared__ double2 sm[];
+  double2* Ub = sm;                         // [M][NB] u_k of the panel's steps
+  double2* Lt = Ub + MX * NB;               // [NB][NB] Lt[k][l] = u_l[p_k], l < k
+  double2* dg = Lt + NB * NB;               // [M] current diagonal
+  double2* zc = dg + MX;                    // [NB] z of the panel's earlier steps for the pivot column
+  double2* colb = zc + NB;                  // [M] current pivot column (panel phase)
+  double2* zsh = colb;                      // [NT/2][NB] z of the columns of a chunk (update phase)
+  double* cc = (double*)(colb + LargeSymSmem::shared_region(MX));  // [2M+2] projection coefficients
+  int* piv = (int*)(cc + 2 * MX + 2);       // [M] pivot of step k
+  int* used = piv + MX;                     // [M] swept
+  int* used0 = used + MX;                   // [M] swept at the start of the panel
+  __shared__ int s_r, s_p, s_status, s_rot;
+  __shared__ unsigned long long s_key[NW], s_cmx[NW], s_cmax;
+  __shared__ int s_idx[NW];
+  __shared__ WgDesc wd;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ctid = rank * NT + tid, CNT = C * NT;
+  const bool draw = (a.upot == nullptr);
+  const bool tmat = (a.mode == kModeTmat);
+  const bool refl = (a.mode == kModeRefl);
+
+  // Block argmax of the diagonal keys over the unswept indices (ties: lowest
+  // index) together with a max of per-thread values `cm`; results in s_p and s_cmax.
+  auto reduce_pivot = [&](unsigned long long best, int bi, unsigned long long cm) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      const unsigned long long oc = __shfl_xor_sync(0xffffffffu, cm, off);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+      cm = oc > cm ? oc : cm;
+    }
+    if (lane == 0) {
+      s_key[warp] = best;
+      s_idx[warp] = bi;
+      s_cmx[warp] = cm;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      best = lane < NW ? s_key[lane] : 0ULL;
+      bi = lane < NW ? s_idx[lane] : 0x7fffffff;
+      cm = lane < NW ? s_cmx[lane] : 0ULL;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        const unsigned long long oc = __shfl_xor_sync(0xffffffffu, cm, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+        cm = oc > cm ? oc : cm;
+      }
+      if (lane == 0) {
+        s_p = (best == 0ULL) ? -1 : bi;  // -1: no usable diagonal left
+        s_cmax = cm;
+      }
+    }
+    __syncthreads();
+  };
+
+  for (;;) {
+    if (rank == 0 && tid == 0) {
+      s_r = atomicAdd(a.work_counter, 1);
+      if (s_r < a.nreal) wd = a.wgs[a.item_wg ? a.item_wg[s_r] : 0];
+    }
+    cluster.sync();
+    if (rank != 0 && tid == 0) {
+      s_r = *cluster.map_shared_rank(&s_r, 0);
+      if (s_r < a.nreal) wd = *cluster.map_shared_rank(&wd, 0);
+    }
+    cluster.sync();  // rank 0's shared memory has been read before any CTA can leave the loop
+    const int r = s_r;
+    if (r >= a.nreal) break;
+    const int M = wd.M, ny = wd.ny;
+    const int64_t mm = (int64_t)M * M;
+    double2* ws = a.work + (int64_t)(blockIdx.x / C) * a.work_stride;
+    double2* W = ws;                              // upper triangle, W[i * M + j], i <= j
+    double2* Rg = ws + mm;
+    double2* Tg = ws + 2 * mm;
+    uint64_t* gen = (uint64_t*)(ws + 3 * mm);     // [ny][4]
+    double* urow_g = (double*)(gen + 4 * ny);     // [ny] paired potential row
+    double2* PR = (double2*)(urow_g + ((ny + 1) & ~1)) + (int64_t)rank * NB * M;  // [NB][M] this CTA's raw pivot columns
+    if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
+    for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    if (draw) {
+      for (int iy = ctid; iy < ny; iy += CNT) {
+        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
+        gen[4 * iy + 0] = st.s0;
+        gen[4 * iy + 1] = st.s1;
+        gen[4 * iy + 2] = st.s2;
+        gen[4 * iy + 3] = st.s3;
+      }
+    }
+    const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;
+    const int ne = a.n_end > 0 ? a.n_end : wd.nx;
+    cluster.sync();
+    // Rank 0's status decides for the whole cluster (every CTA computes the
+    // same flags from the same data; reading one copy makes the decision
+    // uniform by construction).  It is read right after a cluster barrier,
+    // and rank 0 writes it again only after the next one.
+    const int* status0 = cluster.map_shared_rank(&s_status, 0);
+
+    for (int n = 0; n < ne; ++n) {
+      if (*status0 == kStatusNeedPivot) break;
+      const int id = (refl ? wd.nx - 1 - n : n) - wd.nxfree;
+      const bool dis = (id >= 0 && id < wd.nxdiso);
+      if (dis) {
+        // 1. The slice's potential, paired (j, ny-1-j) as sum and difference
+        //    (the transverse grid is symmetric and cos(pi d (1 - y)) =
+        //    (-1)^d cos(pi d y)), then the projection over half the points.
+        const int h = ny >> 1;
+        for (int j = ctid; j < h + (ny & 1); j += CNT) {
+          const int jp = ny - 1 - j;
+          double u0 = 0.0, u1 = 0.0;
+          if (draw) {
+            Xoshiro st{gen[4 * j], gen[4 * j + 1], gen[4 * j + 2], gen[4 * j + 3]};
+            u0 = scaled_normal(wd.stdu, st);
+            gen[4 * j + 0] = st.s0;
+            gen[4 * j + 1] = st.s1;
+            gen[4 * j + 2] = st.s2;
+            gen[4 * j + 3] = st.s3;
+            if (jp != j) {
+              Xoshiro sq{gen[4 * jp], gen[4 * jp + 1], gen[4 * jp + 2], gen[4 * jp + 3]};
+              u1 = scaled_normal(wd.stdu, sq);
+              gen[4 * jp + 0] = sq.s0;
+              gen[4 * jp + 1] = sq.s1;
+              gen[4 * jp + 2] = sq.s2;
+              gen[4 * jp + 3] = sq.s3;
+            }
+          } else {
+            u0 = U[(int64_t)id * a.pot_xstride + (int64_t)j * a.pot_ystride];
+            u1 = U[(int64_t)id * a.pot_xstride + (int64_t)jp * a.pot_ystride];
+          }
+          if (jp == j) {
+            urow_g[j] = u0;
+          } else {
+            urow_g[j] = u0 + u1;
+            urow_g[jp] = u0 - u1;
+          }
+        }
+        cluster.sync();
+        const int nd = 2 * M + 1;
+        for (int d = tid; d < nd; d += NT) {
+          const double* ct = wd.costab + d;
+          const double* up = (d & 1) ? urow_g + (ny - 1) : urow_g;
+          const int us = (d & 1) ? -1 : 1;
+          double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+          int j = 0;
+          for (; j + 4 <= h; j += 4) {
+            s0 = fma(ct[(int64_t)(j + 0) * nd], __ldcg(up + us * (j + 0)), s0);
+            s1 = fma(ct[(int64_t)(j + 1) * nd], __ldcg(up + us * (j + 1)), s1);
+            s2 = fma(ct[(int64_t)(j + 2) * nd], __ldcg(up + us * (j + 2)), s2);
+            s3 = fma(ct[(int64_t)(j + 3) * nd], __ldcg(up + us * (j + 3)), s3);
+          }
+          for (; j < h; ++j) s0 = fma(ct[(int64_t)j * nd], __ldcg(up + us * j), s0);
+          if (ny & 1) s1 = fma(ct[(int64_t)h * nd], __ldcg(urow_g + h), s1);
+          cc[d] = (s0 + s1) + (s2 + s3);
+        }
+        __syncthreads();
+      }
+
+      // 2. X = A_n - V_n - B Gss B on the upper triangle, in place, and
+      //    R = B Gs1 (elements split over the cluster).
+      const double2* adiag = (n == 0 || n == wd.nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
+      const double rsign = (n == 1) ? 1.0 : -1.0;
+      for (int64_t e = ctid; e < mm; e += CNT) {
+        const int i = (int)(e / M), j = (int)(e % M);
+        if (i <= j) {
+          double2 x = (i == j) ? adiag[i] : make_double2(0.0, 0.0);
+          if (dis) x = csub(x, make_double2(cc[j - i] - cc[i + j + 2], 0.0));
+          if (n > 0) x = csub(x, cmul(cmul(wd.bmat[i], __ldcg(W + e)), wd.bmat[j]));
+          W[e] = x;
+        }
+        if (n > 0) Rg[e] = cmul(wd.bmat[i], cscale(rsign, __ldcg(Rg + e)));
+      }
+      cluster.sync();
+      unsigned long long best = 0ULL;
+      int bi = 0x7fffffff;
+      for (int i = tid; i < M; i += NT) {
+        const double2 x = __ldcg(W + (int64_t)i * M + i);
+        dg[i] = x;
+        used[i] = 0;
+        const unsigned long long k = pivot_key(x);
+        if (k > best) {
+          best = k;
+          bi = i;
+        }
+      }
+      reduce_pivot(best, bi, 0ULL);
+
+      // 3. Blocked symmetric Gauss-Jordan.
+      for (int k0 = 0; k0 < M; k0 += NB) {
+        const int nbk = min(NB, M - k0);
+        for (int i = tid; i < M; i += NT) used0[i] = used[i];
+        __syncthreads();
+        for (int kk = 0; kk < nbk; ++kk) {
+          int p = s_p;
+          if (p < 0) {  // zero or NaN diagonal everywhere left: the pivoted kernel decides
+            if (tid == 0) s_status = kStatusNeedPivot;
+            p = 0;
+            while (p < M - 1 && used[p]) ++p;
+          }
+          // a. column p at the panel start: W[i][p] above the diagonal, and
+          //    below it M[i][p] = +-W[p][i], minus when i was swept before the panel
+          for (int i = tid; i < M; i += NT) {
+            double2 v;
+            if (i <= p) {
+              v = __ldcg(W + (int64_t)i * M + p);
+            } else {
+              v = __ldcg(W + (int64_t)p * M + i);
+              if (used0[i]) v = cneg(v);
+            }
+            PR[(int64_t)kk * M + i] = v;
+            colb[i] = v;
+          }
+          __syncthreads();
+          if (kk > 0) {
+            // b. the panel's earlier steps: z_m = x[p_m] + sum_{l<m} u_l[p_m] z_l, x += U z
+            if (tid == 0) {
+              for (int m = 0; m < kk; ++m) {
+                const int pm = piv[k0 + m];
+                double2 v = colb[pm];
+                for (int l = 0; l < m; ++l) v = cfms(v, cneg(Ub[pm * NB + l]), zc[l]);
+                zc[m] = v;
+              }
+            }
+            __syncthreads();
+            for (int i = tid; i < M; i += NT) {
+              double2 x = colb[i];
+              for (int m = 0; m < kk; ++m) x = cfms(x, cneg(Ub[i * NB + m]), zc[m]);
+              colb[i] = x;
+            }
+            __syncthreads();
+          }
+          // c. reciprocal, multipliers, diagonal update; the next pivot and the
+          //    largest unswept entry of this column in one reduction
+          const double2 z = colb[p];
+          const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
+          const double2 d = make_double2(z.x * rden, -z.y * rden);
+          unsigned long long nbest = 0ULL, cm = 0ULL;
+          int nbi = 0x7fffffff;
+          for (int i = tid; i < M; i += NT) {
+            const double2 g = colb[i];
+            double2 u;
+            if (i == p) {
+              u = make_double2(d.x - 1.0, d.y);
+            } else {
+              u = cneg(cmul(g, d));
+            }
+            Ub[i * NB + kk] = u;
+            if (!used[i] && i != p) {
+              const unsigned long long kc = pivot_key(g);
+              cm = kc > cm ? kc : cm;
+              const double2 nd2 = cfms(dg[i], cneg(u), g);  // dg + u g
+              dg[i] = nd2;
+              const unsigned long long kd = pivot_key(nd2);
+              if (kd > nbest) {
+                nbest = kd;
+                nbi = i;
+              }
+            }
+          }
+          reduce_pivot(nbest, nbi, cm);
+          if (tid == 0) {
+            const double zmag = __longlong_as_double((long long)pivot_key(z));
+            const double omag = __longlong_as_double((long long)s_cmax);
+            if (!(zmag > 0.0) || zmag < a.sym_tau * omag) s_status = kStatusNeedPivot;
+            used[p] = 1;
+            piv[k0 + kk] = p;
+          }
+          __syncthreads();
+        }
+        for (int e = tid; e < nbk * nbk; e += NT) {
+          const int k = e / nbk, l = e % nbk;
+          Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
+        }
+        __syncthreads();
+
+        // d. The panel applied to every column of [W | R].  Units 0..M-1 are
+        //    the W columns (rows i <= j), M..2M-1 the R columns; they are dealt
+        //    round-robin to the cluster's CTAs and, inside a CTA, in zigzag
+        //    order over the chunk rounds so that the triangle's long and short
+        //    columns share threads.  T threads share a unit's rows when a CTA
+        //    has fewer units than threads; its z then goes through shared memory.
+        const int ncl = (2 * M - rank + C - 1) / C;
+        int T = 1;
+        while (T < kSymMaxRowSplit && ncl * T * 2 <= NT) T *= 2;
+        const int NCH = NT / T;
+        const int cs = tid % NCH, sub = tid / NCH;
+        for (int c0 = 0, rr = 0; c0 < ncl; c0 += NCH, ++rr) {
+          const int c = c0 + ((rr & 1) ? NCH - 1 - cs : cs);
+          const bool active = c < ncl;
+          const int u = rank + C * c;
+          int kind = 0, j = 0, mcol = -1, len = 0;  // kind 0: W column, 1: W pivot column, 2: R column
+          double2* col = nullptr;
+          if (active) {
+            if (u < M) {
+              j = u;
+              col = W + j;
+              len = j + 1;
+              if (used[j] && !used0[j]) {
+                kind = 1;
+                for (int m = 0; m < nbk; ++m)
+                  if (piv[k0 + m] == j) mcol = m;
+              }
+            } else {
+              kind = 2;
+              j = u - M;
+              col = Rg + j;
+              len = M;
+            }
+          }
+          double2 zz[NB];
+#pragma unroll
+          for (int k = 0; k < NB; ++k) zz[k] = make_double2(0.0, 0.0);
+          if (active && sub == 0) {
+            if (kind == 1) {
+              // pivot column m: x = u_m + e_{p_m}; only the later steps act on it
+#pragma unroll
+              for (int l = 0; l < NB; ++l) {
+                if (l > mcol && l < nbk) {
+                  double2 v = Lt[l * NB + mcol];
+#pragma unroll
+                  for (int q = 0; q < NB; ++q)
+                    if (q > mcol && q < l) v = cfms(v, cneg(Lt[l * NB + q]), zz[q]);
+                  zz[l] = v;
+                }
+              }
+            } else {
+              const double sg = (kind == 0 && used0[j]) ? -1.0 : 1.0;
+#pragma unroll
+              for (int m = 0; m < NB; ++m) {
+                if (m < nbk) {
+                  double2 v = (kind == 0) ? cscale(sg, __ldcg(PR + (int64_t)m * M + j))
+                                          : __ldcg(col + (int64_t)piv[k0 + m] * M);
+#pragma unroll
+                  for (int l = 0; l < m; ++l) v = cfms(v, cneg(Lt[m * NB + l]), zz[l]);
+                  zz[m] = v;
+                }
+              }
+            }
+            if (T > 1) {
+#pragma unroll
+              for (int k = 0; k < NB; ++k) zsh[cs * NB + k] = zz[k];
+            }
+          }
+          if (T > 1) {
+            __syncthreads();  // z is read before any row of these columns changes
+            if (active) {
+#pragma unroll
+              for (int k = 0; k < NB; ++k) zz[k] = zsh[cs * NB + k];
+            }
+          }
+          if (active) {
+            for (int i = sub; i < len; i += T) {
+              const double2* ui = Ub + i * NB;
+              double2 x;
+              if (kind == 1) {
+                x = ui[mcol];
+                if (i == j) x.x += 1.0;
+              } else {
+                x = __ldcg(col + (int64_t)i * M);
+              }
+              if (nbk == NB) {
+#pragma unroll
+                for (int k = 0; k < NB; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
+              } else {
+                for (int k = 0; k < nbk; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
+              }
+              col[(int64_t)i * M] = x;
+            }
+          }
+          if (T > 1) __syncthreads();  // zsh is reused by the next chunk
+        }
+        cluster.sync();
+      }
+    }
+
+    if (*status0 == kStatusNeedPivot) {
+      cluster.sync();  // every CTA has read the flag before rank 0 moves on
+      if (rank == 0 && tid == 0) {
+        a.status[r] = kStatusNeedPivot;
+        a.flag_list[atomicAdd(a.work_counter + 1, 1)] = r;
+      }
+      cluster.sync();
+      continue;
+    }
+    if (ne < wd.nx) {  // stopped early (timing proxy): no Fisher-Lee stage
+      __syncthreads();
+      if (rank == 0 && tid == 0) a.status[r] = s_status;
+      cluster.sync();
+      continue;
+    }
+
+    if (refl) {
+      // Reflection from the reverse sweep: G11 = W (symmetric, upper triangle),
+      // r = -1 + 2i sqrt(real mu) G11 sqrt(real mu) (src/waveguide.f90:510-512).
+      double2* rout = a.tout + (int64_t)r * M * M;
+      for (int e = ctid; e < M * M; e += CNT) {
+        const int i = e % M, j = e / M;
+        const double2 gij = __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i));
+        const double2 v = cmul(cmul(wd.sqmu_r[i], gij), wd.sqmu_r[j]);
+        rout[e] = make_double2((i == j ? -1.0 : 0.0) - 2.0 * v.y, 2.0 * v.x);
+      }
+      __syncthreads();
+      if (rank == 0 && tid == 0) a.status[r] = s_status;
+      cluster.sync();
+      continue;
+    }
+
+    // 5. Fisher-Lee from R (natural order): t = 2i sqmu Gs1 sqmu, Gs1 = sign R,
+    //    into the workspace, column-major (ld = nrow).
+    const double gsign = (wd.nx >= 2) ? -1.0 : 1.0;
+    const int row0 = tmat ? 0 : wd.row0, col0 = tmat ? 0 : wd.col0;
+    const int nrow = tmat ? M : wd.nrow, ncol = tmat ? M : wd.ncol;
+    const double2* sqmu = tmat ? wd.sqmu_r : wd.sqmu_c;
+    double2* tout = a.tout ? a.tout + (int64_t)r * nrow * ncol : nullptr;
+    for (int e = ctid; e < nrow * ncol; e += CNT) {
+      const int i = e % nrow, j = e / nrow;
+      const int gi = row0 + i, gj = col0 + j;
+      const double2 g = cscale(gsign, __ldcg(Rg + (int64_t)gi * M + gj));
+      const double2 v = cmul(cmul(sqmu[gi], g), sqmu[gj]);
+      const double2 t = make_double2(-2.0 * v.y, 2.0 * v.x);
+      Tg[e] = t;
+      if (tout) tout[e] = t;
+    }
+    cluster.sync();
+
+    if (!tmat) {
+      // 6. Eigenvalues of t^H t: one-sided Jacobi on the vectors of the
+      //    smaller dimension, in the workspace; the pairs of a round are
+      //    split over the cluster's warps.
+      const bool bycol = nrow >= ncol;
+      const int nv = bycol ? ncol : nrow;
+      const int L = bycol ? nrow : ncol;
+      const int es = bycol ? 1 : nrow;
+      const int vs = bycol ? nrow : 1;
+      const int NP = (nv + 1) & ~1;
+      const double tol = 2.220446049250313e-16 * L;
+      int* rot0 = cluster.map_shared_rank(&s_rot, 0);
+      int sweep = 0;
+      for (; sweep < 60; ++sweep) {
+        if (rank == 0 && tid == 0) s_rot = 0;
+        cluster.sync();
+        for (int rr = 0; rr < NP - 1; ++rr) {
+          for (int pk = rank * NW + warp; pk < NP / 2; pk += C * NW) {
+            const int pos1 = pk, pos2 = NP - 1 - pk;
+            const int vp = pos1 == 0 ? 0 : ((pos1 - 1 + rr) % (NP - 1)) + 1;
+            const int vq = ((pos2 - 1 + rr) % (NP - 1)) + 1;
+            if (vp >= nv || vq >= nv) continue;
+            double2* xp = Tg + (int64_t)vp * vs;
+            double2* xq = Tg + (int64_t)vq * vs;
+            double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+            for (int i = lane; i < L; i += 32) {
+              const double2 u = __ldcg(xp + (int64_t)i * es), w = __ldcg(xq + (int64_t)i * es);
+              al = fma(u.x, u.x, fma(u.y, u.y, al));
+              be = fma(w.x, w.x, fma(w.y, w.y, be));
+              gr = fma(u.x, w.x, fma(u.y, w.y, gr));
+              gi = fma(u.x, w.y, fma(-u.y, w.x, gi));
+            }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              al += __shfl_xor_sync(0xffffffffu, al, off);
+              be += __shfl_xor_sync(0xffffffffu, be, off);
+              gr += __shfl_xor_sync(0xffffffffu, gr, off);
+              gi += __shfl_xor_sync(0xffffffffu, gi, off);
+            }
+            const double ga = sqrt(gr * gr + gi * gi);
+            if (ga > tol * sqrt(al * be) && ga > 1e-300) {
+              if (lane == 0) atomicOr(rot0, 1);
+              const double zeta = (be - al) / (2.0 * ga);
+              const double t = fabs(zeta) > 1e100 ? 0.5 / zeta
+                                                  : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+              const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+              const double2 ph = make_double2(gr / ga, -gi / ga);
+              for (int i = lane; i < L; i += 32) {
+                const double2 u = __ldcg(xp + (int64_t)i * es);
+                const double2 w = cmul(ph, __ldcg(xq + (int64_t)i * es));
+                xp[(int64_t)i * es] = make_double2(c * u.x - s * w.x, c * u.y - s * w.y);
+                xq[(int64_t)i * es] = make_double2(s * u.x + c * w.x, s * u.y + c * w.y);
+              }
+            }
+          }
+          cluster.sync();
+        }
+        const int any = *rot0;
+        cluster.sync();  // every CTA has read the flag before rank 0 clears it
+        if (!any) break;
+      }
+      if (sweep == 60 && tid == 0 && s_status == RG_OK) s_status = RG_ERR_NOCONV;
+      if (rank == 0) {
+        for (int k = warp; k < nv; k += NW) {
+          const double2* xk = Tg + (int64_t)k * vs;
+          double s = 0.0;
+          for (int i = lane; i < L; i += 32) {
+            const double2 u = __ldcg(xk + (int64_t)i * es);
+            s = fma(u.x, u.x, fma(u.y, u.y, s));
+          }
+#pragma unroll
+          for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+          if (lane == 0) cc[k] = s;
+        }
+        __syncthreads();
+        const int64_t obase = a.teig_off ? a.teig_off[r] : (int64_t)r * wd.neigv;
+        for (int k = tid; k < nv; k += NT) {
+          const double tk = cc[k];
+          int rank_k = 0;
+          for (int j = 0; j < nv; ++j) {
+            const double tj = cc[j];
+            rank_k += (tj > tk || (tj == tk && j < k)) ? 1 : 0;
+          }
+          if (rank_k < wd.neigv) a.teig[obase + rank_k] = tk;
+        }
+      }
+    }
+    __syncthreads();
+    if (rank == 0 && tid == 0) a.status[r] = s_status;
+    cluster.sync();  // the cluster finishes this item before rank 0 takes the next
+  }
+}
+
+}  // namespace
+
+// Same cluster-size policy as the pivoted blocked kernel (sweep_large_plan).
+int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
+  const size_t smem = LargeSymSmem::bytes(a.max_M);
+  if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes for the symmetric large-mode kernel");
+  RG_CUDA(cudaFuncSetAttribute(sweep_large_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_large_sym_kernel, kSymNT, smem));
+  if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "symmetric large-mode sweep kernel does not fit on an SM");
+  const int slots = per_sm * sm_count;
+  int C = 1;
+  if (a.force_cluster > 0) {
+    while (C < kSymMaxCluster && C < a.force_cluster) C *= 2;
+  } else {
+    while (C < kSymMaxCluster && (int64_t)a.nreal * C * 2 <= slots) C *= 2;
+  }
+  int nclusters = slots / C;
+  if (C > 1) {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = C;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C * 64);
+    cfg.blockDim = dim3(kSymNT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int maxc = 0;
+    RG_CUDA(cudaOccupancyMaxActiveClusters(&maxc, sweep_large_sym_kernel, &cfg));
+    if (maxc < 1) {
+      C = 1;
+      nclusters = slots;
+    } else {
+      nclusters = maxc;
+    }
+  }
+  if (nclusters > a.nreal) nclusters = a.nreal;
+  if (nclusters < 1) nclusters = 1;
+  a.cluster = C;
+  *grid = nclusters * C;
+  *work_stride = large_sym_stride(a.max_M, a.max_ny);
+  return RG_OK;
+}
+
+int launch_sweep_large_sym(const SweepArgs& a, cudaStream_t stream, int grid) {
+  if (a.nreal <= 0) return RG_OK;
+  const size_t smem = LargeSymSmem::bytes(a.max_M);
+  const int C = a.cluster > 0 ? a.cluster : 1;
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute attr{};
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = C;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kSymNT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  RG_CUDA(cudaLaunchKernelEx(&cfg, sweep_large_sym_kernel, a));
+  return RG_OK;
+}
+
+}  // namespace rg

@@ -459,7 +459,7 @@ rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
   a.work_counter = w->d_counter;
   a.max_M = w->nmu;
   a.max_ny = w->ny;
-  a.symmetric = (w->p.boundtype == RG_BOUND_DIRICHLET && w->nmu <= rg::kMaxModesSmem && symmetric_enabled()) ? 1 : 0;
+  a.symmetric = (w->p.boundtype == RG_BOUND_DIRICHLET && symmetric_enabled()) ? 1 : 0;
   a.sym_tau = symmetric_tau();
   return a;
 }
@@ -666,9 +666,9 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   RG_CUDA(cudaGraphLaunch(w->graph, s));
   RG_CUDA(cudaEventRecord(w->ev_sweep1, s));
   w->sweep_timed = true;
-  w->last_batch.kernel = (a.force_large || a.max_M > rg::kMaxModesSmem) ? RG_KERNEL_BLOCKED
-                         : a.symmetric                                 ? RG_KERNEL_SYMMETRIC
-                                                                       : RG_KERNEL_PIVOTED;
+  const bool blocked = a.force_large || a.max_M > rg::kMaxModesSmem;
+  w->last_batch.kernel = blocked ? (a.symmetric ? RG_KERNEL_BLOCKED_SYMMETRIC : RG_KERNEL_BLOCKED)
+                                 : (a.symmetric ? RG_KERNEL_SYMMETRIC : RG_KERNEL_PIVOTED);
   w->last_batch.grid = grid;
   w->last_batch.cluster = a.cluster > 0 ? a.cluster : 1;
   w->last_batch.rerun = 0;
@@ -1079,7 +1079,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     // periodic ones straight to the pivoted kernel).
     bool any_dirichlet = false;
     for (int k = k0; k < k1; ++k) any_dirichlet = any_dirichlet || !descs[o_wg[k]].periodic;
-    a.symmetric = (maxM <= rg::kMaxModesSmem && any_dirichlet && symmetric_enabled()) ? 1 : 0;
+    a.symmetric = (any_dirichlet && symmetric_enabled()) ? 1 : 0;
     a.sym_tau = symmetric_tau();
     int grid = 0;
     if ((rc = place_workspace(w0, a, 0, &grid))) break;
@@ -1169,7 +1169,7 @@ int rg_last_batch_info(rg_waveguide* w, rg_batch_info* info) {
   DeviceGuard g(w->device);
   RG_CUDA(cudaEventSynchronize(w->ev_sweep1));
   *info = w->last_batch;
-  if (info->kernel == RG_KERNEL_SYMMETRIC) {
+  if (info->kernel == RG_KERNEL_SYMMETRIC || info->kernel == RG_KERNEL_BLOCKED_SYMMETRIC) {
     int32_t flagged = 0;
     RG_CUDA(cudaMemcpyAsync(&flagged, w->d_counter + 1, sizeof flagged, cudaMemcpyDeviceToHost, w->stream));
     RG_CUDA(cudaStreamSynchronize(w->stream));

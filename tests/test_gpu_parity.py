@@ -295,7 +295,7 @@ def test_large_autotuned_cluster_matches():
     g = rg.Waveguide(**kw)
     seeds = np.arange(1, 9, dtype=np.int32)
     b = g.tdistrib_batch(seeds)  # autotuned cluster size
-    assert g.last_batch_info()["kernel"] == "blocked"
+    assert g.last_batch_info()["kernel"] in ("blocked", "blocked_symmetric")
     for k, s in enumerate(seeds[:3]):
         one = np.zeros(s * g.neigv)
         g.compute_tdistrib(int(s), one)  # single realization: cluster of 8

@@ -35,6 +35,16 @@ SYM_CASES = {
 }
 
 
+# Blocked kernel (M > 64): short guides keep the oracle fast.
+LARGE_SYM = {
+    "m72": dict(boundtype="dirichlet", nxdiso=30, nxfree=2, wol=36.25, exfac=1.0, aratio=1.0, dscat=6.0, ny=96),
+    "m100_ragged_abs": dict(boundtype="dirichlet", nxdiso=20, nxfree=0, wol=50.25, exfac=1.0, aratio=1.0,
+                            dscat=8.0, dabso=1.0, napera=0.7, naperb=0.9, ny=200),
+    "m128": dict(boundtype="dirichlet", nxdiso=16, nxfree=0, wol=64.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=512),
+    "m256": dict(boundtype="dirichlet", nxdiso=4, nxfree=0, wol=128.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=1024),
+}
+
+
 @pytest.fixture(autouse=True)
 def _no_autotune(monkeypatch):
     monkeypatch.setenv("RG_AUTOTUNE", "0")
@@ -51,7 +61,10 @@ def batch(kw, seeds, monkeypatch, symmetric=True, tau=None):
     g = rg.Waveguide(**kw)
     out = g.tdistrib_batch(seeds)
     info = g.last_batch_info()
-    assert info["kernel"] == ("symmetric" if symmetric else "pivoted")
+    if g.nmu > 64:
+        assert info["kernel"] == ("blocked_symmetric" if symmetric else "blocked")
+    else:
+        assert info["kernel"] == ("symmetric" if symmetric else "pivoted")
     return out.reshape(len(seeds), g.neigv), info
 
 
@@ -134,3 +147,64 @@ def test_multi_mixed_boundaries(monkeypatch):
         one = np.zeros(s * g.neigv)
         g.compute_tdistrib(s, one)
         np.testing.assert_array_equal(T, one[(s - 1) * g.neigv:])
+
+
+@pytest.mark.parametrize("name", sorted(LARGE_SYM))
+def test_blocked_symmetric_matches_pivoted_and_oracle(name, monkeypatch):
+    kw = LARGE_SYM[name]
+    seeds = np.arange(1, 13, dtype=np.int32)
+    bs, info = batch(kw, seeds, monkeypatch, symmetric=True)
+    bg, _ = batch(kw, seeds, monkeypatch, symmetric=False)
+    assert info["rerun"] == 0
+    assert np.max(np.abs(bs - bg)) <= KERNEL_ABS, name
+    o = O.Waveguide(**kw)
+    ref = o.tdistrib_upot(o.potential(int(seeds[3])))
+    assert np.max(np.abs(bs[3] - ref)) <= TN_ABS, name
+
+
+def test_blocked_symmetric_t_r_and_single_call(monkeypatch):
+    """t and r through the blocked symmetric kernel (r from the reverse
+    sweep on a materialised potential), and a single call equals the batch."""
+    monkeypatch.setenv("RG_SYMMETRIC", "1")
+    kw = LARGE_SYM["m72"]
+    o, g = O.Waveguide(**kw), rg.Waveguide(**kw)
+    u = o.potential(5)
+    ro, to = o.refl_trans_v1_upot(u)
+    r, t = g.refl_trans_v1_upot(u, want_r=True)
+    assert np.linalg.norm(t - to) / np.linalg.norm(to) <= T_REL
+    assert np.linalg.norm(r - ro) / np.linalg.norm(ro) <= T_REL
+    d = t.conj().T @ t + r.conj().T @ r - np.eye(g.nmu)
+    assert np.linalg.norm(d) < 1e-9  # flux conservation at dabso = 0
+    seeds = np.array([3, 8], np.int32)
+    b = g.tdistrib_batch(seeds)
+    for k, s in enumerate(seeds):
+        one = np.zeros(s * g.neigv)
+        g.compute_tdistrib(int(s), one)
+        np.testing.assert_array_equal(b[k * g.neigv:(k + 1) * g.neigv], one[(s - 1) * g.neigv:])
+
+
+def test_blocked_every_item_flagged_reruns_bit_identical(monkeypatch):
+    kw = LARGE_SYM["m128"]
+    seeds = np.arange(1, 7, dtype=np.int32)
+    bg, _ = batch(kw, seeds, monkeypatch, symmetric=False)
+    ball, info = batch(kw, seeds, monkeypatch, symmetric=True, tau=1e300)
+    assert info["rerun"] == len(seeds)
+    np.testing.assert_array_equal(ball, bg)
+
+
+def test_blocked_multi_mixed_boundaries(monkeypatch):
+    """The blocked class with Dirichlet and periodic guides of different sizes."""
+    monkeypatch.setenv("RG_SYMMETRIC", "1")
+    specs = [LARGE_SYM["m72"],
+             dict(boundtype="periodic", nxdiso=12, nxfree=0, wol=40.3, exfac=1.0, aratio=1.0, dscat=4.0),
+             LARGE_SYM["m100_ragged_abs"]]
+    gs = [rg.Waveguide(**kw) for kw in specs]
+    items = [(gs[k % 3], 1 + k) for k in range(6)]
+    res, st = rg.tdistrib_multi(items, return_status=True)
+    assert np.all(st == 0)
+    for (g, s), T in zip(items, res):
+        one = np.zeros(s * g.neigv)
+        g.compute_tdistrib(s, one)
+        np.testing.assert_array_equal(T, one[(s - 1) * g.neigv:])
+    o = O.Waveguide(**specs[1])
+    assert np.max(np.abs(res[1] - o.tdistrib_upot(o.potential(2)))) <= TN_ABS
