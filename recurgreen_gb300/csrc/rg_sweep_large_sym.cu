@@ -22,7 +22,9 @@
 // W and R stay in natural order, so there is no permutation bookkeeping.
 // The z of a W column comes from the panel's raw pivot columns, which each
 // CTA keeps in its own staging area: no column reads another column's
-// storage during the update, so one cluster barrier per panel suffices.
+// storage during the update.  A cluster barrier separates each panel's
+// factorisation (whose column fetches read W anywhere) from its update, and
+// another ends the update.
 //
 // A diagonal pivot below sym_tau times the largest unswept entry of its
 // column flags the realization (kStatusNeedPivot, appended to flag_list);
@@ -47,7 +49,7 @@ constexpr int kSymMaxRowSplit = 8;
 // share one region: they are never live at the same time.
 struct LargeSymSmem {
   __host__ __device__ static size_t shared_region(int M) {
-    const size_t z = (size_t)(kSymNT / 2) * kSymNB;
+    const size_t z = (size_t)(kSymNT / 4) * 2 * kSymNB;
     return (size_t)M > z ? (size_t)M : z;
   }
   static size_t bytes(int M) {
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
   double2* dg = Lt + NB * NB;               // [M] current diagonal
   double2* zc = dg + MX;                    // [NB] z of the panel's earlier steps for the pivot column
   double2* colb = zc + NB;                  // [M] current pivot column (panel phase)
-  double2* zsh = colb;                      // [NT/2][NB] z of the columns of a chunk (update phase)
+  double2* zsh = colb;                      // [NT/4][2][NB] z of the units of a chunk (update phase)
   double* cc = (double*)(colb + LargeSymSmem::shared_region(MX));  // [2M+2] projection coefficients
   int* piv = (int*)(cc + 2 * MX + 2);       // [M] pivot of step k
   int* used = piv + MX;                     // [M] swept
@@ -163,12 +165,20 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
     if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
     for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
     if (draw) {
-      for (int iy = ctid; iy < ny; iy += CNT) {
-        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
-        gen[4 * iy + 0] = st.s0;
-        gen[4 * iy + 1] = st.s1;
-        gen[4 * iy + 2] = st.s2;
-        gen[4 * iy + 3] = st.s3;
+      // Each generator state is set up by the thread that draws from it (the
+      // pair (j, ny-1-j) below), so it is only ever read and written from one
+      // SM: a state written by another CTA could be read through a stale L1
+      // line when the cluster takes its next item.
+      for (int j = ctid; j < (ny >> 1) + (ny & 1); j += CNT) {
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int iy = h2 == 0 ? j : ny - 1 - j;
+          if (h2 == 1 && iy == j) break;
+          const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
+          gen[4 * iy + 0] = st.s0;
+          gen[4 * iy + 1] = st.s1;
+          gen[4 * iy + 2] = st.s2;
+          gen[4 * iy + 3] = st.s3;
+        }
       }
     }
     const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;
@@ -354,103 +364,165 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           const int k = e / nbk, l = e % nbk;
           Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
         }
-        __syncthreads();
+        // The panel's column fetches read W anywhere (row p_k lies in other
+        // columns), so no CTA of the cluster may start writing W until every
+        // CTA has finished factoring the panel.
+        if (C > 1) cluster.sync();
+        else __syncthreads();
 
-        // d. The panel applied to every column of [W | R].  Units 0..M-1 are
-        //    the W columns (rows i <= j), M..2M-1 the R columns; they are dealt
-        //    round-robin to the cluster's CTAs and, inside a CTA, in zigzag
-        //    order over the chunk rounds so that the triangle's long and short
-        //    columns share threads.  T threads share a unit's rows when a CTA
-        //    has fewer units than threads; its z then goes through shared memory.
-        const int ncl = (2 * M - rank + C - 1) / C;
-        int T = 1;
-        while (T < kSymMaxRowSplit && ncl * T * 2 <= NT) T *= 2;
-        const int NCH = NT / T;
-        const int cs = tid % NCH, sub = tid / NCH;
-        for (int c0 = 0, rr = 0; c0 < ncl; c0 += NCH, ++rr) {
-          const int c = c0 + ((rr & 1) ? NCH - 1 - cs : cs);
-          const bool active = c < ncl;
-          const int u = rank + C * c;
-          int kind = 0, j = 0, mcol = -1, len = 0;  // kind 0: W column, 1: W pivot column, 2: R column
-          double2* col = nullptr;
-          if (active) {
-            if (u < M) {
-              j = u;
-              col = W + j;
-              len = j + 1;
-              if (used[j] && !used0[j]) {
-                kind = 1;
-                for (int m = 0; m < nbk; ++m)
-                  if (piv[k0 + m] == j) mcol = m;
-              }
-            } else {
-              kind = 2;
-              j = u - M;
-              col = Rg + j;
-              len = M;
-            }
-          }
-          double2 zz[NB];
+        // d. The panel applied to every column of [W | R]: a column gets
+        //    x += U z over its rows (i <= j for W, all for R), with
+        //    z = (I - L)^-1 x[p] from its pivot rows (for W, the panel's raw
+        //    pivot columns with the sign rule), and the panel's pivot column
+        //    m is u_m + e_{p_m} with the later steps applied.
+        auto column_z = [&](int kind, int j, int mcol, const double2* col, double2* zz) {
 #pragma unroll
           for (int k = 0; k < NB; ++k) zz[k] = make_double2(0.0, 0.0);
-          if (active && sub == 0) {
-            if (kind == 1) {
-              // pivot column m: x = u_m + e_{p_m}; only the later steps act on it
+          if (kind == 1) {
 #pragma unroll
-              for (int l = 0; l < NB; ++l) {
-                if (l > mcol && l < nbk) {
-                  double2 v = Lt[l * NB + mcol];
+            for (int l = 0; l < NB; ++l) {
+              if (l > mcol && l < nbk) {
+                double2 v = Lt[l * NB + mcol];
 #pragma unroll
-                  for (int q = 0; q < NB; ++q)
-                    if (q > mcol && q < l) v = cfms(v, cneg(Lt[l * NB + q]), zz[q]);
-                  zz[l] = v;
-                }
-              }
-            } else {
-              const double sg = (kind == 0 && used0[j]) ? -1.0 : 1.0;
-#pragma unroll
-              for (int m = 0; m < NB; ++m) {
-                if (m < nbk) {
-                  double2 v = (kind == 0) ? cscale(sg, __ldcg(PR + (int64_t)m * M + j))
-                                          : __ldcg(col + (int64_t)piv[k0 + m] * M);
-#pragma unroll
-                  for (int l = 0; l < m; ++l) v = cfms(v, cneg(Lt[m * NB + l]), zz[l]);
-                  zz[m] = v;
-                }
+                for (int q = 0; q < NB; ++q)
+                  if (q > mcol && q < l) v = cfms(v, cneg(Lt[l * NB + q]), zz[q]);
+                zz[l] = v;
               }
             }
-            if (T > 1) {
+          } else {
+            const double sg = (kind == 0 && used0[j]) ? -1.0 : 1.0;
 #pragma unroll
-              for (int k = 0; k < NB; ++k) zsh[cs * NB + k] = zz[k];
+            for (int m = 0; m < NB; ++m) {
+              if (m < nbk) {
+                double2 v = (kind == 0) ? cscale(sg, __ldcg(PR + (int64_t)m * M + j))
+                                        : __ldcg(col + (int64_t)piv[k0 + m] * M);
+#pragma unroll
+                for (int l = 0; l < m; ++l) v = cfms(v, cneg(Lt[m * NB + l]), zz[l]);
+                zz[m] = v;
+              }
             }
           }
-          if (T > 1) {
+        };
+        // Rows sub, sub+T, ... < len of one column, two rows per iteration
+        // (two independent FMA chains, two loads in flight).
+        auto column_rows = [&](int kind, int j, int mcol, double2* col, int len, const double2* zz, int sub, int T) {
+          auto init = [&](int i) {
+            if (kind == 1) {
+              double2 x = Ub[i * NB + mcol];
+              if (i == j) x.x += 1.0;
+              return x;
+            }
+            return __ldcg(col + (int64_t)i * M);
+          };
+          int i = sub;
+          if (nbk == NB) {
+            for (; i + T < len; i += 2 * T) {
+              const double2* u0 = Ub + i * NB;
+              const double2* u1 = Ub + (i + T) * NB;
+              double2 x0 = init(i), x1 = init(i + T);
+#pragma unroll
+              for (int k = 0; k < NB; ++k) {
+                x0 = cfms(x0, cneg(u0[k]), zz[k]);
+                x1 = cfms(x1, cneg(u1[k]), zz[k]);
+              }
+              col[(int64_t)i * M] = x0;
+              col[(int64_t)(i + T) * M] = x1;
+            }
+          }
+          for (; i < len; i += T) {
+            const double2* ui = Ub + i * NB;
+            double2 x = init(i);
+            for (int k = 0; k < nbk; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
+            col[(int64_t)i * M] = x;
+          }
+        };
+        // Which kind of W column j is: 1 if it is pivot mcol of this panel.
+        auto w_kind = [&](int j, int* mcol) {
+          *mcol = -1;
+          if (used[j] && !used0[j]) {
+            for (int m = 0; m < nbk; ++m)
+              if (piv[k0 + m] == j) *mcol = m;
+            return 1;
+          }
+          return 0;
+        };
+        // Units: the W column pairs (q, M-1-q), M+1 rows together, then the
+        // R columns (M rows), dealt round-robin to the cluster's CTAs.  T
+        // threads share a unit's rows (T = 1, 4 or 8, whichever gives the
+        // fewest rows per thread); with T > 1 the unit's z vectors (two for
+        // a pair) come through shared memory, [NT/4][2][NB] at most.
+        const int P = (M + 1) / 2;
+        const int ucta = (P + M - rank + C - 1) / C;
+        int T = 1;
+        {
+          int best = ((ucta + NT - 1) / NT) * (M + 1);
+          for (int t = 4; t <= kSymMaxRowSplit; t *= 2) {
+            const int rows = ((ucta + NT / t - 1) / (NT / t)) * ((M + 1 + t - 1) / t);
+            if (rows < best) {
+              best = rows;
+              T = t;
+            }
+          }
+        }
+        const int NCH = NT / T;
+        const int cs = tid % NCH, sub = tid / NCH;
+        for (int c0 = 0; c0 < ucta; c0 += NCH) {
+          const int c = c0 + cs;
+          const bool active = c < ucta;
+          const int u = rank + C * c;
+          int ka = 0, kb = 0, ja = 0, jb = 0, ma = -1, mb = -1, lena = 0, lenb = 0;
+          double2* cola = nullptr;
+          double2* colb2 = nullptr;
+          if (active) {
+            if (u < P) {
+              ja = u;
+              jb = M - 1 - u;
+              lena = ja + 1;
+              lenb = (jb != ja) ? jb + 1 : 0;
+              cola = W + ja;
+              colb2 = W + jb;
+              ka = w_kind(ja, &ma);
+              if (lenb) kb = w_kind(jb, &mb);
+            } else {
+              ka = 2;
+              ja = u - P;
+              lena = M;
+              cola = Rg + ja;
+            }
+          }
+          double2 za[NB], zb[NB];
+          if (T == 1) {
+            if (active) {
+              column_z(ka, ja, ma, cola, za);
+              column_rows(ka, ja, ma, cola, lena, za, 0, 1);
+              if (lenb) {
+                column_z(kb, jb, mb, colb2, zb);
+                column_rows(kb, jb, mb, colb2, lenb, zb, 0, 1);
+              }
+            }
+          } else {
+            if (active && sub < 2 && (sub == 0 || lenb)) {
+              double2 zz[NB];
+              if (sub == 0) column_z(ka, ja, ma, cola, zz);
+              else column_z(kb, jb, mb, colb2, zz);
+#pragma unroll
+              for (int k = 0; k < NB; ++k) zsh[(cs * 2 + sub) * NB + k] = zz[k];
+            }
             __syncthreads();  // z is read before any row of these columns changes
             if (active) {
 #pragma unroll
-              for (int k = 0; k < NB; ++k) zz[k] = zsh[cs * NB + k];
-            }
-          }
-          if (active) {
-            for (int i = sub; i < len; i += T) {
-              const double2* ui = Ub + i * NB;
-              double2 x;
-              if (kind == 1) {
-                x = ui[mcol];
-                if (i == j) x.x += 1.0;
-              } else {
-                x = __ldcg(col + (int64_t)i * M);
-              }
-              if (nbk == NB) {
+              for (int k = 0; k < NB; ++k) za[k] = zsh[(cs * 2) * NB + k];
+              // the unit's virtual rows v = sub, sub+T, ...: column a, then column b
+              column_rows(ka, ja, ma, cola, lena, za, sub, T);
+              if (lenb) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
-              } else {
-                for (int k = 0; k < nbk; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
+                for (int k = 0; k < NB; ++k) zb[k] = zsh[(cs * 2 + 1) * NB + k];
+                const int i0 = ((sub - lena) % T + T) % T;
+                column_rows(kb, jb, mb, colb2, lenb, zb, i0, T);
               }
-              col[(int64_t)i * M] = x;
             }
+            __syncthreads();  // zsh is reused by the next chunk
           }
-          if (T > 1) __syncthreads();  // zsh is reused by the next chunk
         }
         cluster.sync();
       }

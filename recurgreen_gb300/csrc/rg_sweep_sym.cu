@@ -97,12 +97,18 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
       for (int b = 0; b < CB; ++b)
         R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? 1.0 : 0.0, 0.0);
     if (draw) {
-      for (int iy = tid; iy < ny; iy += NT) {
-        const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
-        gen[4 * iy + 0] = st.s0;
-        gen[4 * iy + 1] = st.s1;
-        gen[4 * iy + 2] = st.s2;
-        gen[4 * iy + 3] = st.s3;
+      // Each generator state is set up by the thread that draws from it (the
+      // pair (j, ny-1-j) of the projection step).
+      for (int j = tid; j < (ny >> 1) + (ny & 1); j += NT) {
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int iy = h2 == 0 ? j : ny - 1 - j;
+          if (h2 == 1 && iy == j) break;
+          const Xoshiro st = jump_state(seeded_state(a.seeds[r]), wd.jumppoly + 4 * (int64_t)iy);
+          gen[4 * iy + 0] = st.s0;
+          gen[4 * iy + 1] = st.s1;
+          gen[4 * iy + 2] = st.s2;
+          gen[4 * iy + 3] = st.s3;
+        }
       }
     }
     const double* U = draw ? nullptr : a.upot + (int64_t)r * a.pot_rstride;

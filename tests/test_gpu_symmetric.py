@@ -208,3 +208,17 @@ def test_blocked_multi_mixed_boundaries(monkeypatch):
         np.testing.assert_array_equal(T, one[(s - 1) * g.neigv:])
     o = O.Waveguide(**specs[1])
     assert np.max(np.abs(res[1] - o.tdistrib_upot(o.potential(2)))) <= TN_ABS
+
+
+@pytest.mark.parametrize("wol,ny", [(36.25, 96), (64.25, 512)])
+def test_blocked_symmetric_clusters_take_several_items(wol, ny, monkeypatch):
+    """Batch sizes that give 8- and 4-CTA clusters with more items than
+    co-resident clusters, so each cluster takes a second item: every CTA's
+    generator states must be its own (no stale state from the last item)."""
+    kw = dict(boundtype="dirichlet", nxdiso=3, nxfree=0, wol=wol, exfac=1.0, aratio=1.0, dscat=5.0, ny=ny)
+    for n in (20, 60):
+        seeds = np.arange(1, n + 1, dtype=np.int32)
+        bs, info = batch(kw, seeds, monkeypatch, symmetric=True)
+        bg, _ = batch(kw, seeds, monkeypatch, symmetric=False)
+        assert info["cluster"] > 1
+        assert np.max(np.abs(bs - bg)) <= KERNEL_ABS, (n, info)
