@@ -403,37 +403,42 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
             }
           }
         };
-        // Rows sub, sub+T, ... < len of one column, two rows per iteration
-        // (two independent FMA chains, two loads in flight).
-        auto column_rows = [&](int kind, int j, int mcol, double2* col, int len, const double2* zz, int sub, int T) {
-          auto init = [&](int i) {
-            if (kind == 1) {
-              double2 x = Ub[i * NB + mcol];
-              if (i == j) x.x += 1.0;
+        // The rows of a unit as one sequence of virtual rows v = sub, sub+T,
+        // ... < lena + lenb: v < lena is row v of column a, the rest row
+        // v - lena of column b.  A pair unit has M+1 virtual rows and an R
+        // unit M, so the threads of a warp (consecutive units) run the same
+        // trip count and their FP64 instructions keep every lane busy.
+        struct Col {
+          int kind, j, mcol, len;
+          double2* col;
+        };
+        auto unit_rows = [&](const Col& A, const double2* za, const Col& B, const double2* zb, int sub, int T) {
+          const int tot = A.len + B.len;
+          // the starting value of virtual row v and where it goes
+          auto load = [&](int v, int* irow, double2** dst) {
+            const bool inA = v < A.len;
+            const Col& c = inA ? A : B;
+            const int i = inA ? v : v - A.len;
+            *irow = i;
+            *dst = c.col + (int64_t)i * M;
+            if (c.kind == 1) {
+              double2 x = Ub[i * NB + c.mcol];
+              if (i == c.j) x.x += 1.0;
               return x;
             }
-            return __ldcg(col + (int64_t)i * M);
+            return __ldcg(*dst);
           };
-          int i = sub;
-          if (nbk == NB) {
-            for (; i + T < len; i += 2 * T) {
-              const double2* u0 = Ub + i * NB;
-              const double2* u1 = Ub + (i + T) * NB;
-              double2 x0 = init(i), x1 = init(i + T);
-#pragma unroll
-              for (int k = 0; k < NB; ++k) {
-                x0 = cfms(x0, cneg(u0[k]), zz[k]);
-                x1 = cfms(x1, cneg(u1[k]), zz[k]);
-              }
-              col[(int64_t)i * M] = x0;
-              col[(int64_t)(i + T) * M] = x1;
-            }
-          }
-          for (; i < len; i += T) {
+          int v = sub;
+          for (; v < tot; v += T) {
+            int i;
+            double2* d;
+            double2 x = load(v, &i, &d);
+            const bool a0 = v < A.len;
             const double2* ui = Ub + i * NB;
-            double2 x = init(i);
-            for (int k = 0; k < nbk; ++k) x = cfms(x, cneg(ui[k]), zz[k]);
-            col[(int64_t)i * M] = x;
+#pragma unroll
+            for (int k = 0; k < NB; ++k)
+              if (k < nbk) x = cfms(x, cneg(ui[k]), a0 ? za[k] : zb[k]);
+            *d = x;
           }
         };
         // Which kind of W column j is: 1 if it is pivot mcol of this panel.
@@ -490,15 +495,16 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
               cola = Rg + ja;
             }
           }
+          const Col A{ka, ja, ma, lena, cola};
+          const Col B{kb, jb, mb, lenb, colb2 ? colb2 : cola};
           double2 za[NB], zb[NB];
+#pragma unroll
+          for (int k = 0; k < NB; ++k) zb[k] = make_double2(0.0, 0.0);
           if (T == 1) {
             if (active) {
               column_z(ka, ja, ma, cola, za);
-              column_rows(ka, ja, ma, cola, lena, za, 0, 1);
-              if (lenb) {
-                column_z(kb, jb, mb, colb2, zb);
-                column_rows(kb, jb, mb, colb2, lenb, zb, 0, 1);
-              }
+              if (lenb) column_z(kb, jb, mb, colb2, zb);
+              unit_rows(A, za, B, zb, 0, 1);
             }
           } else {
             if (active && sub < 2 && (sub == 0 || lenb)) {
@@ -512,14 +518,11 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
             if (active) {
 #pragma unroll
               for (int k = 0; k < NB; ++k) za[k] = zsh[(cs * 2) * NB + k];
-              // the unit's virtual rows v = sub, sub+T, ...: column a, then column b
-              column_rows(ka, ja, ma, cola, lena, za, sub, T);
               if (lenb) {
 #pragma unroll
                 for (int k = 0; k < NB; ++k) zb[k] = zsh[(cs * 2 + 1) * NB + k];
-                const int i0 = ((sub - lena) % T + T) % T;
-                column_rows(kb, jb, mb, colb2, lenb, zb, i0, T);
               }
+              unit_rows(A, za, B, zb, sub, T);
             }
             __syncthreads();  // zsh is reused by the next chunk
           }
