@@ -95,3 +95,25 @@ def test_segmented_forward_matches_one_sweep():
     gs1 = dump[0, -1, 1].cpu().numpy()
     tt = 2j * sq[:, None] * gs1 * sq[None, :]
     assert np.linalg.norm(tt - t1) / np.linalg.norm(t1) <= 1e-12
+
+
+def test_both_gradients_in_one_sweep_match_autograd():
+    """transmission_losses_and_grads (two cotangent chains in one reverse
+    sweep) equals two torch.autograd.grad calls through transmission_losses."""
+    torch = pytest.importorskip("torch")
+    from recurgreen_gb300.adjoint import transmission_losses, transmission_losses_and_grads
+
+    kw = dict(boundtype="dirichlet", nxdiso=20, nxfree=1, wol=8.25, exfac=1.0, aratio=1.0, dscat=4.0, dabso=0.2,
+              ny=32)
+    g = rg.Waveguide(**kw)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    U = torch.randn(3, g.nxdiso, g.ny, dtype=torch.float64, device="cuda", generator=gen) * g.stdu
+    U.requires_grad_(True)
+    L1, L2 = transmission_losses(U, g, 5)
+    (a1,) = torch.autograd.grad(L1.sum(), U, retain_graph=True)
+    (a2,) = torch.autograd.grad(L2.sum(), U)
+    M1, M2, d1, d2 = transmission_losses_and_grads(U.detach(), g, 5)
+    assert torch.equal(M1, L1.detach()) and torch.equal(M2, L2.detach())
+    for ref, got in ((a1, d1), (a2, d2)):
+        assert (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item() <= 1e-12
