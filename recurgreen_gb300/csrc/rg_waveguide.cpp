@@ -1081,6 +1081,23 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     for (int k = k0; k < k1; ++k) any_dirichlet = any_dirichlet || !descs[o_wg[k]].periodic;
     a.symmetric = (any_dirichlet && symmetric_enabled()) ? 1 : 0;
     a.sym_tau = symmetric_tau();
+    if (maxM > rg::kMaxModesSmem) {
+      // The blocked class's makespan is at least its longest item's time on
+      // one CTA slot.  When that item's work times the slot count exceeds the
+      // class's total work, spread every item over a cluster (the items are
+      // ordered longest first, so the long ones start at once).
+      double total = 0.0, longest = 0.0;
+      for (int k = k0; k < k1; ++k) {
+        const rg::WgDesc& d = descs[o_wg[k]];
+        const double wk = (double)d.M * d.M * d.M * d.nx;
+        total += wk;
+        longest = std::max(longest, wk);
+      }
+      const double slots = 2.0 * w0->sm_count;  // two CTAs per SM
+      int C = 1;
+      while (C < 8 && longest * slots / C > total) C *= 2;
+      a.force_cluster = C > 1 ? C : 0;
+    }
     int grid = 0;
     if ((rc = place_workspace(w0, a, 0, &grid))) break;
     e = cudaMemsetAsync(w0->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);

@@ -32,6 +32,10 @@ def _noalloc(g, seed, torch):
 @pytest.mark.parametrize("kw", [
     dict(boundtype="dirichlet", nxdiso=200, nxfree=0, wol=5.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=64),
     dict(boundtype="dirichlet", nxdiso=300, nxfree=2, wol=32.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=256),
+    # above 64 modes: the blocked symmetric kernel's matrices and staging share the array
+    dict(boundtype="dirichlet", nxdiso=12, nxfree=1, wol=64.25, exfac=1.0, aratio=1.0, dscat=5.0, ny=512),
+    # periodic: the pivoted kernel
+    dict(boundtype="periodic", nxdiso=40, nxfree=0, wol=6.3, exfac=1.0, aratio=1.0, dscat=2.0),
 ])
 def test_noalloc_matches_allocating_entry_point(kw):
     torch = pytest.importorskip("torch")
