@@ -77,7 +77,7 @@ struct SweepArgs {
   const double2* state_in;    // [nreal][2][M][M] (Gss, Gs1) after slice n_begin-1, natural order; nullptr: fresh start
   double2* state_dump;        // [nreal][n_end-n_begin][2][M][M] (Gss, Gs1) after every slice, optional
   double2* state_out;         // [nreal][2][M][M] state after slice n_end-1, optional
-  int force_large;            // 1: use the blocked global-memory kernel even for max_M <= 64 (autotuner)
+  int force_large;            // 1: the pivoted blocked kernel even for max_M <= 64 (segment mode with states)
   // Symmetric sweep (Dirichlet items): the symmetric kernel (shared-memory
   // or blocked, by max_M) runs every item and appends those it cannot pivot
   // stably to flag_list; the pivoted kernel of the same class re-runs them.
@@ -87,7 +87,8 @@ struct SweepArgs {
   // Queue indirection of the pivoted kernel (set by launch_sweep for the re-run):
   const int32_t* item_idx;    // [count] item index of queue position q; nullptr: q itself
   const int* count_ptr;       // device-side queue length; nullptr: nreal
-  int force_cluster;          // > 0: cluster size for the blocked kernel instead of the heuristic (autotuner)
+  int force_cluster;          // > 0: cluster size for the blocked kernels instead of the heuristic
+                              // (autotuner, multi calls with long items)
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were
