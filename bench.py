@@ -72,7 +72,7 @@ def flops_symmetric(M: int, nx: int) -> float:
 
 
 KERNEL_NAMES = {"symmetric": "sweep_sym_kernel<64,256,2>", "pivoted": "sweep_kernel<64,256,2>",
-                "blocked": "sweep_large_kernel"}
+                "blocked": "sweep_large_kernel", "blocked_symmetric": "sweep_large_sym_kernel"}
 
 
 def config(batch: int) -> dict:
@@ -361,6 +361,7 @@ def main() -> None:
     import torch.distributed as dist
 
     import recurgreen_gb300 as rg
+    from recurgreen_gb300 import replicas
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -408,9 +409,7 @@ def main() -> None:
     clocks = clk.stop()
     dt = e0.elapsed_time(e1) / 1e3
     if world > 1:
-        t = torch.tensor([dt], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+        dt = replicas.max_over_ranks(dt)
         dist.barrier()
     bad = int((st_d != 0).sum().item())
 
@@ -428,9 +427,7 @@ def main() -> None:
             raise rg.RecurGreenError(rc, L.rg_last_error().decode())
     e2e_dt = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([e2e_dt], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_dt = float(t.item())
+        e2e_dt = replicas.max_over_ranks(e2e_dt)
     per = None
     if args.per_sample > 0 and rank == 0:
         pr, pdt = _per_realization(L, w, list(seeds_h[: args.per_sample]), np)

@@ -158,17 +158,23 @@ def linear_bins(nbins: int, xmin: float = 0.0, xmax: float = 1.0) -> np.ndarray:
     return np.array([xmin + (xmax - xmin) * (i - 1) / nbins for i in range(1, nbins + 2)], np.float64)
 
 
-def density(samples, bins):
-    """histogram (GPU) + eps/10 + normalize_histogram + moving_average:
-    returns (rho_data[nbins, 2] = (centre, density), missing)."""
-    histo, missing = histogram(samples, bins)
-    histo = histo + np.finfo(np.float64).eps / 10.0
+def density_from_counts(histo, bins):
+    """eps/10 + normalize_histogram + moving_average (src/main.f90:243-245,
+    src/base_utils.f90:524-570) on histogram counts: rho_data[nbins, 2] =
+    (centre, density)."""
+    histo = np.asarray(histo, np.float64) + np.finfo(np.float64).eps / 10.0
     npoints = 0.0
     for v in histo:  # sum(histo): sequential, as the Fortran intrinsic
         npoints += v
     rho = np.array([histo[j] / (npoints * (bins[j + 1] - bins[j])) for j in range(histo.size)])
     centres = np.array([(0.0 + bins[j] + bins[j + 1]) / 2 for j in range(histo.size)])
-    return np.stack([centres, rho], axis=1), missing
+    return np.stack([centres, rho], axis=1)
+
+
+def density(samples, bins):
+    """histogram (GPU) then density_from_counts: (rho_data[nbins, 2], missing)."""
+    histo, missing = histogram(samples, bins)
+    return density_from_counts(histo, bins), missing
 
 
 def prepare_distrib(tallvals, nbins: int):
@@ -237,8 +243,13 @@ def read_real_array(path: str) -> np.ndarray:
     return np.array(out, np.float64)
 
 
-def task_tdistrib(settings: dict, outdir: str = "out") -> dict:
-    """task_tdistrib (src/main.f90:73-123) with the seed loop as one GPU batch."""
+def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
+    """task_tdistrib (src/main.f90:73-123) with the seed loop as one GPU batch.
+
+    With a torch.distributed process group, each rank (one GPU) takes a
+    contiguous range of the seeds; the histogram counts are summed over the
+    ranks and rank 0 writes the files (see replicas.py).  Other ranks return
+    the same rho and missing values with no file paths."""
     wg = settings["waveguide"]
     td = settings["tdistrib"]
     w = Waveguide(boundtype=str(wg.get("boundtype", "dirichlet")).strip(), nxdiso=int(wg["nxdiso"]),
@@ -246,6 +257,8 @@ def task_tdistrib(settings: dict, outdir: str = "out") -> dict:
                   aratio=float(wg.get("aratio", 1.0)), dscat=float(wg["dscat"]), dabso=float(wg.get("dabso", 0.0)),
                   napera=float(wg.get("napera", 1.0)), naperb=float(wg.get("naperb", 1.0)), ny=int(wg.get("ny", 0)))
     nseed, nbins = int(td["nseed"]), int(td["nbins"])
+    if group is not None:
+        return _task_tdistrib_replicas(w, td, nseed, nbins, outdir, group)
     t0 = time.perf_counter()
     tallvals = w.tdistrib_batch(np.arange(1, nseed + 1, dtype=np.int32))
     tsec = time.perf_counter() - t0
@@ -260,6 +273,34 @@ def task_tdistrib(settings: dict, outdir: str = "out") -> dict:
         epath = unique_filename(os.path.join(ddir, "result_"), ".eigvals.csv")
         save_raw_eigvals(epath, tallvals, pre)
         res["eigvals"] = epath
+    return res
+
+
+def _task_tdistrib_replicas(w: Waveguide, td: dict, nseed: int, nbins: int, outdir: str, group) -> dict:
+    import torch.distributed as dist
+
+    from . import replicas
+
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    seeds = replicas.seed_range(rank, world, nseed)
+    t0 = time.perf_counter()
+    local = w.tdistrib_batch(seeds) if seeds.size else np.zeros(0)
+    tsec = replicas.max_over_ranks(time.perf_counter() - t0, group)
+    bins = chebyshev_bins(nbins)
+    histo, missing = histogram(local, bins) if local.size else (np.zeros(nbins), 0.0)
+    histo, missing = replicas.sum_counts(histo, missing, group)
+    rho = density_from_counts(histo, bins)
+    tallvals = replicas.gather_values(local, group) if td.get("save_eigvals", False) else None
+    res = {"distrib": None, "tallvals": tallvals, "rho": rho, "missing": missing, "time": tsec}
+    if rank == 0:
+        ddir = os.path.join(generate_directory(w, outdir), "distrib")
+        os.makedirs(ddir, exist_ok=True)
+        pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec)
+        res["distrib"] = unique_filename(os.path.join(ddir, "result_"), ".distrib.csv")
+        save_distrib(res["distrib"], rho, pre)
+        if tallvals is not None:
+            res["eigvals"] = unique_filename(os.path.join(ddir, "result_"), ".eigvals.csv")
+            save_raw_eigvals(res["eigvals"], tallvals, pre)
     return res
 
 

@@ -108,3 +108,21 @@ def test_task_tdistrib_end_to_end(tmp_path):
     np.testing.assert_allclose(res["rho"], rho_o, rtol=1e-13, atol=0)
     eig = open(res["eigvals"]).read().splitlines()
     assert eig[5] == "%% Transmission eigenvalues (400 values)" and len(eig) == 6 + 400
+
+
+@pytest.mark.gpu
+def test_task_tdistrib_replica_path_matches(tmp_path):
+    """The sharded path of task_tdistrib (a process group; here one gloo rank
+    on one GPU) writes the same distribution as the single-process path."""
+    import torch.distributed as dist
+
+    g = T.read_namelists(NML)
+    plain = T.task_tdistrib(g, str(tmp_path / "plain"))
+    dist.init_process_group("gloo", store=dist.HashStore(), rank=0, world_size=1)
+    try:
+        rep = T.task_tdistrib(g, str(tmp_path / "rep"), group=dist.group.WORLD)
+    finally:
+        dist.destroy_process_group()
+    np.testing.assert_array_equal(rep["rho"], plain["rho"])
+    np.testing.assert_array_equal(rep["tallvals"], plain["tallvals"])
+    assert open(rep["distrib"]).read().splitlines()[5:] == open(plain["distrib"]).read().splitlines()[5:]
