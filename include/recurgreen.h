@@ -109,6 +109,15 @@ int rg_compute_tdistrib(rg_waveguide* wg, int iseed, double* tallvals, int64_t l
  * extra matrix products per slice. */
 int rg_compute_refl_trans_v1(rg_waveguide* wg, int iseed, double* rmat, double* tmat);
 
+/* compute_refl_trans_v1 for many seeds (the loop of the tpattern task,
+ * src/main.f90:796-830): for k < n, t and r of seed seeds[k] go to
+ * tmat + 2*k*nmu*nmu and rmat + 2*k*nmu*nmu (host, column-major complex;
+ * rmat may be NULL).  The realizations run in batched launches of bounded
+ * device memory.  status[k] (may be NULL) receives each realization's status;
+ * returns the first non-OK one after all have run. */
+int rg_refl_trans_v1_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* rmat, double* tmat,
+                           int32_t* status);
+
 /* As rg_compute_tdistrib / rg_compute_refl_trans_v1, but for a caller-given
  * potential upot(nxdiso, ny) (host, column-major: x fastest), already scaled
  * by stdu as set_hamiltonian_waveguide stores it (src/waveguide.f90:366-372).

@@ -168,6 +168,19 @@ class Waveguide {
     return out;
   }
 
+  // compute_refl_trans_v1 for many seeds (the tpattern loop,
+  // src/main.f90:796-830): t and r of seeds[k] at offset k*nmu*nmu of tmat
+  // and rmat (each matrix column-major); rmat may be null.
+  void refl_trans_v1_batch(const std::vector<int32_t>& seeds, std::vector<std::complex<double>>* rmat,
+                           std::vector<std::complex<double>>& tmat) {
+    const size_t n = seeds.size() * (size_t)get_nmu() * get_nmu();
+    tmat.resize(n);
+    if (rmat) rmat->resize(n);
+    check(rg_refl_trans_v1_batch(h_, seeds.data(), (int)seeds.size(),
+                                 rmat ? reinterpret_cast<double*>(rmat->data()) : nullptr,
+                                 reinterpret_cast<double*>(tmat.data()), nullptr));
+  }
+
   // print_parameters (src/waveguide.f90:1003-1018): three lines, each
   // starting with `prefix`.
   void print_parameters(std::FILE* fp, const std::string& prefix) const {

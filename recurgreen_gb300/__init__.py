@@ -27,7 +27,7 @@ EXPORTS = (
     "rg_compute_tdistrib", "rg_compute_refl_trans_v1", "rg_tdistrib_upot", "rg_refl_trans_v1_upot",
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
     "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi", "rg_sweep_segment",
-    "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info",
+    "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info", "rg_refl_trans_v1_batch",
 )
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
 
@@ -85,6 +85,7 @@ def lib() -> C.CDLL:
     L.rg_adjoint_grad_rows.argtypes = [vp, vp, C.c_int, vp, i64, vp]
     L.rg_get_modes.argtypes = [vp, vp, vp]
     L.rg_last_batch_info.argtypes = [vp, C.POINTER(rg_batch_info)]
+    L.rg_refl_trans_v1_batch.argtypes = [vp, ip, C.c_int, vp, vp, ip]
     _LIB = L
     return L
 
@@ -190,6 +191,19 @@ class Waveguide:
         r = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
         _check(lib().rg_compute_refl_trans_v1(self._h, int(iseed), r.ctypes.data, t.ctypes.data))
         return r, t
+
+    def refl_trans_v1_batch(self, seeds, want_r: bool = True):
+        """compute_refl_trans_v1 for many seeds in batched launches: (r, t),
+        each of shape (n, nmu, nmu) (r is None without want_r)."""
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        n, M = seeds.size, self.nmu
+        t = np.zeros((n, M, M), np.complex128)  # each matrix column-major: t[k] holds t^T
+        r = np.zeros((n, M, M), np.complex128) if want_r else None
+        st = np.zeros(n, np.int32)
+        ip = C.POINTER(C.c_int32)
+        _check(lib().rg_refl_trans_v1_batch(self._h, seeds.ctypes.data_as(ip), n, r.ctypes.data if want_r else None,
+                                             t.ctypes.data, st.ctypes.data_as(ip)))
+        return (r.transpose(0, 2, 1) if want_r else None), t.transpose(0, 2, 1)
 
     def tdistrib_upot(self, upot: np.ndarray, want_t: bool = False):
         """Eigenvalues (and the filtered Fisher-Lee t) for a given potential

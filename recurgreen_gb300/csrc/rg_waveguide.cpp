@@ -894,6 +894,89 @@ int rg_compute_tdistrib(rg_waveguide* w, int iseed, double* tallvals, int64_t le
   return run_single(w, &s, nullptr, rg::kModeEig, tallvals + (iseed - 1) * (int64_t)w->neigv, nullptr, nullptr);
 }
 
+int rg_refl_trans_v1_batch(rg_waveguide* w, const int32_t* seeds, int n, double* rmat, double* tmat,
+                           int32_t* status) {
+  if (!w || n < 0 || (n > 0 && (!seeds || !tmat)))
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_batch: invalid argument");
+  if (n == 0) return RG_OK;
+  DeviceGuard g(w->device);
+  const int M = w->nmu;
+  const size_t mm = (size_t)M * M;
+  const size_t pot_per = (size_t)w->p.nxdiso * w->ny;
+  const bool want_r = rmat != nullptr;
+  // Realizations per launch: their potentials (drawn first, so that r's
+  // reverse sweep can read the rows backwards) and t, r within ~1 GiB.
+  const size_t per_item = sizeof(double) * pot_per + sizeof(double2) * mm * (want_r ? 2 : 1);
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, ((size_t)1 << 30) / per_item));
+  const size_t b_seed = align256(sizeof(int32_t) * chunk), b_st = align256(sizeof(int32_t) * 2 * chunk);
+  const size_t b_pot = align256(sizeof(double) * pot_per * chunk), b_mat = align256(sizeof(double2) * mm * chunk);
+  char* buf = nullptr;
+  RG_CUDA(cudaMalloc((void**)&buf, b_seed + b_st + b_pot + b_mat * (want_r ? 2 : 1)));
+  int32_t* d_seed = (int32_t*)buf;
+  int32_t* d_st = (int32_t*)(buf + b_seed);
+  double* d_pot = (double*)(buf + b_seed + b_st);
+  double2* d_t = (double2*)(buf + b_seed + b_st + b_pot);
+  double2* d_r = want_r ? (double2*)(buf + b_seed + b_st + b_pot + b_mat) : nullptr;
+  std::vector<int32_t> st(2 * (size_t)chunk);
+  cudaStream_t s = w->stream;
+  int rc = RG_OK, bad = RG_OK;
+  for (int k0 = 0; !rc && k0 < n; k0 += chunk) {
+    const int nk = std::min(chunk, n - k0);
+    cudaError_t e = cudaMemcpyAsync(d_seed, seeds + k0, sizeof(int32_t) * nk, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      rc = rg::cuda_fail(e, "rg_refl_trans_v1_batch seeds");
+      break;
+    }
+    rg::PotArgs pa{};
+    pa.nxdiso = w->p.nxdiso;
+    pa.ny = w->ny;
+    pa.nreal = nk;
+    pa.stdu = w->stdu;
+    pa.seeds = d_seed;
+    pa.jumppoly = w->d_jump;
+    pa.upot = d_pot;
+    if ((rc = rg::launch_potential(pa, s))) break;
+    for (int pass = 0; pass < (want_r ? 2 : 1) && !rc; ++pass) {
+      rg::SweepArgs a = make_args(w, pass == 0 ? rg::kModeTmat : rg::kModeRefl);
+      a.nreal = nk;
+      a.upot = d_pot;
+      a.pot_rstride = (int64_t)pot_per;
+      a.pot_xstride = w->ny;
+      a.pot_ystride = 1;
+      a.tout = pass == 0 ? d_t : d_r;
+      a.status = d_st + (size_t)pass * chunk;
+      int grid = 0;
+      if ((rc = place_workspace(w, a, 0, &grid))) break;
+      e = cudaMemsetAsync(w->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);
+      if (e != cudaSuccess) {
+        rc = rg::cuda_fail(e, "rg_refl_trans_v1_batch counter");
+        break;
+      }
+      rc = rg::launch_sweep(a, s, grid);
+    }
+    if (rc) break;
+    e = cudaMemcpyAsync(tmat + 2 * mm * (size_t)k0, d_t, sizeof(double2) * mm * nk, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && want_r)
+      e = cudaMemcpyAsync(rmat + 2 * mm * (size_t)k0, d_r, sizeof(double2) * mm * nk, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), d_st, sizeof(int32_t) * 2 * chunk, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      rc = rg::cuda_fail(e, "rg_refl_trans_v1_batch");
+      break;
+    }
+    for (int k = 0; k < nk; ++k) {
+      const int sk = st[k] != RG_OK ? st[k] : (want_r ? st[(size_t)chunk + k] : RG_OK);
+      if (status) status[k0 + k] = sk;
+      if (!bad && sk != RG_OK) bad = sk;
+    }
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(buf);
+  if (rc) return rc;
+  if (bad) return rg::fail(bad, status_text(bad));
+  return RG_OK;
+}
+
 int rg_tdistrib_upot(rg_waveguide* w, const double* upot, double* teigvals, double* tfilt) {
   if (!w || !upot || !teigvals) return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_upot: NULL argument");
   return run_single(w, nullptr, upot, rg::kModeEig, teigvals, nullptr, tfilt);

@@ -413,11 +413,11 @@ void write_preamble(std::FILE* fp, const recurgreen::Waveguide& w, long nseed, l
                format_g0(tsec, 6).c_str(), format_g0(speed, 6).c_str());
 }
 
-void task_tdistrib(const std::string& text, const std::string& root) {
+// The &waveguide group (src/main.f90:83), plus the optional ny.
+recurgreen::Parameters waveguide_parameters(const std::string& text) {
   const NmlGroup wg = read_namelist(text, "waveguide",
                                     {"boundtype", "wol", "exfac", "dscat", "dabso", "aratio", "nxdiso", "nxfree",
                                      "napera", "naperb", "ny"});
-  const NmlGroup td = read_namelist(text, "tdistrib", {"nseed", "nbins", "nthreads", "save_eigvals"});
   recurgreen::Parameters p;
   p.boundtype = nml_string(wg, "boundtype", "dirichlet");
   p.wol = nml_real(wg, "wol", 0.0);
@@ -430,6 +430,12 @@ void task_tdistrib(const std::string& text, const std::string& root) {
   p.napera = nml_real(wg, "napera", 1.0);
   p.naperb = nml_real(wg, "naperb", 1.0);
   p.ny = (int)nml_int(wg, "ny", 0);
+  return p;
+}
+
+void task_tdistrib(const std::string& text, const std::string& root) {
+  const recurgreen::Parameters p = waveguide_parameters(text);
+  const NmlGroup td = read_namelist(text, "tdistrib", {"nseed", "nbins", "nthreads", "save_eigvals"});
   const long nseed = nml_int(td, "nseed", 0);
   const long nbins = nml_int(td, "nbins", 0);
   const long nthreads = nml_int(td, "nthreads", 1);
@@ -485,14 +491,85 @@ void task_tdistrib(const std::string& text, const std::string& root) {
   }
 }
 
+// task_tpattern (src/main.f90:735-877) for probatype 'incident' and 'total':
+// the mean over seeds of |t_{b,imu}|^2, |r_{b,imu}|^2 or of their column sums.
+void task_tpattern(const std::string& text, const std::string& root) {
+  const NmlGroup tp = read_namelist(text, "tpattern", {"nseed", "imode", "nthreads", "probatype"});
+  const long nseed = nml_int(tp, "nseed", 0);
+  const long imode = nml_int(tp, "imode", 1);
+  const std::string probatype = nml_string(tp, "probatype", "incident");
+  if (nseed <= 0)
+    throw Stop("Invalid number of disorder realizations (received " + fmt_int(nseed) + "), aborting...");
+  if (probatype != "incident" && probatype != "total" && probatype != "deposition")
+    throw Stop("Invalid probatype, received '" + probatype + "', expected incident/total/deposition, aborting...");
+  if (probatype == "deposition")
+    throw Stop("probatype 'deposition' needs the full Green function, which this GPU build does not compute, "
+               "aborting...");
+  recurgreen::Waveguide w(waveguide_parameters(text));
+  const int M = w.get_nmu();
+  const long imu = w.get_parameters().boundtype == "periodic" ? (imode + M / 2 - 1) % M + 1 : imode;
+  if (imu < 1 || imu > M)
+    throw Stop("Invalid incident mode imode=" + fmt_int(imode) + ", expected in [1, " + fmt_int(M) + "], aborting...");
+  std::vector<double> tsum(M, 0.0), rsum(M, 0.0);
+  const auto t0 = std::chrono::steady_clock::now();
+  const long chunk = 256;
+  std::vector<std::complex<double>> t, r;
+  for (long s0 = 1; s0 <= nseed; s0 += chunk) {
+    std::vector<int32_t> seeds;
+    for (long sd = s0; sd < s0 + chunk && sd <= nseed; ++sd) seeds.push_back((int32_t)sd);
+    w.refl_trans_v1_batch(seeds, &r, t);
+    const size_t mm = (size_t)M * M;
+    for (size_t k = 0; k < seeds.size(); ++k) {  // seed order, as the Fortran sum over dim=2
+      const std::complex<double>* tk = t.data() + k * mm;
+      const std::complex<double>* rk = r.data() + k * mm;
+      auto prob = [](std::complex<double> z) {  // abs(z)**2, as the reference writes it
+        const double a = std::abs(z);
+        return a * a;
+      };
+      for (int b = 0; b < M; ++b) {
+        double tp = 0.0, rp = 0.0;
+        if (probatype == "incident") {
+          tp = prob(tk[(size_t)(imu - 1) * M + b]);
+          rp = prob(rk[(size_t)(imu - 1) * M + b]);
+        } else {  // column b summed over its rows
+          for (int i = 0; i < M; ++i) {
+            tp += prob(tk[(size_t)b * M + i]);
+            rp += prob(rk[(size_t)b * M + i]);
+          }
+        }
+        tsum[b] += tp;
+        rsum[b] += rp;
+      }
+    }
+  }
+  const double tsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  const std::string dir = w.generate_directory(root) + "tpattern/";
+  create_directory(dir);
+  const std::string fname = unique_filename(dir + "result_", ".csv");
+  std::FILE* fp = std::fopen(fname.c_str(), "w");
+  if (!fp) throw Stop("Cannot open file: " + fname);
+  std::fprintf(fp, "%%%% Computed on %s by %s\n", timestamp().c_str(), kProgram);
+  w.print_parameters(fp, "%%");
+  std::fprintf(fp, "%%%% Radiation pattern parameters: probatype='%s', nseed=%ld, imode=%ld, time=%s s.\n",
+               probatype.c_str(), nseed, imode, f0(tsec, 3).c_str());
+  std::fprintf(fp, "imu, tprob, rprob\n");
+  for (int b = 0; b < M; ++b)
+    std::fprintf(fp, "%d, %s, %s\n", b + 1, format_g0(tsum[b] / nseed).c_str(), format_g0(rsum[b] / nseed).c_str());
+  std::fclose(fp);
+  std::printf("%sAverage profiles written in file: %s\n", tag_info().c_str(), fname.c_str());
+}
+
 // execute_file (src/main.f90:41-65).
 void execute_file(const std::string& text, const std::string& root) {
   const NmlGroup s = read_namelist(text, "settings", {"task"});
   const std::string task = nml_string(s, "task", "");
   if (task == "tdistrib") {
     task_tdistrib(text, root);
-  } else if (task == "wavefunction" || task == "tprofile" || task == "tprofile_group" || task == "tpattern") {
-    throw Stop("Task '" + task + "' is not part of this GPU build, which runs the tdistrib task, aborting...");
+  } else if (task == "tpattern") {
+    task_tpattern(text, root);
+  } else if (task == "wavefunction" || task == "tprofile" || task == "tprofile_group") {
+    throw Stop("Task '" + task + "' is not part of this GPU build, which runs the tdistrib and tpattern tasks, "
+               "aborting...");
   } else {
     throw Stop("Unknown task '" + task + "', aborting...");
   }

@@ -9,7 +9,7 @@ preamble, a `tm, rho` header, values written like Fortran's G0.16).  The
 eigenvalues come from one batched GPU launch (rg_tdistrib_batch) and the
 histogram counts from the GPU (rg_histogram).
 
-    python -m recurgreen_gb300.tdistrib settings.nml [--outdir DIR]
+    python -m recurgreen_gb300.tdistrib settings.nml [--outdir DIR]     (task tdistrib or tpattern)
     python -m recurgreen_gb300.tdistrib --replot plothisto_settings.nml result_1.eigvals.csv
 """
 from __future__ import annotations
@@ -250,12 +250,8 @@ def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
     contiguous range of the seeds; the histogram counts are summed over the
     ranks and rank 0 writes the files (see replicas.py).  Other ranks return
     the same rho and missing values with no file paths."""
-    wg = settings["waveguide"]
     td = settings["tdistrib"]
-    w = Waveguide(boundtype=str(wg.get("boundtype", "dirichlet")).strip(), nxdiso=int(wg["nxdiso"]),
-                  nxfree=int(wg.get("nxfree", 0)), wol=float(wg["wol"]), exfac=float(wg.get("exfac", 1.0)),
-                  aratio=float(wg.get("aratio", 1.0)), dscat=float(wg["dscat"]), dabso=float(wg.get("dabso", 0.0)),
-                  napera=float(wg.get("napera", 1.0)), naperb=float(wg.get("naperb", 1.0)), ny=int(wg.get("ny", 0)))
+    w = _waveguide_from(settings["waveguide"])
     nseed, nbins = int(td["nseed"]), int(td["nbins"])
     if group is not None:
         return _task_tdistrib_replicas(w, td, nseed, nbins, outdir, group)
@@ -304,6 +300,69 @@ def _task_tdistrib_replicas(w: Waveguide, td: dict, nseed: int, nbins: int, outd
     return res
 
 
+def _waveguide_from(wg: dict) -> Waveguide:
+    return Waveguide(boundtype=str(wg.get("boundtype", "dirichlet")).strip(), nxdiso=int(wg["nxdiso"]),
+                     nxfree=int(wg.get("nxfree", 0)), wol=float(wg["wol"]), exfac=float(wg.get("exfac", 1.0)),
+                     aratio=float(wg.get("aratio", 1.0)), dscat=float(wg["dscat"]), dabso=float(wg.get("dabso", 0.0)),
+                     napera=float(wg.get("napera", 1.0)), naperb=float(wg.get("naperb", 1.0)), ny=int(wg.get("ny", 0)))
+
+
+def tpattern_probabilities(w: Waveguide, nseed: int, imu: int, probatype: str, chunk: int = 256):
+    """The seed loop of task_tpattern (src/main.f90:796-836): the mean over
+    seeds 1..nseed of |t_{b,imu}|^2 and |r_{b,imu}|^2 ('incident') or of
+    sum_b |t_{ba}|^2 and sum_b |r_{ba}|^2 ('total'), from batched t and r."""
+    M = w.nmu
+    tsum, rsum = np.zeros(M), np.zeros(M)
+    for s0 in range(1, nseed + 1, chunk):
+        seeds = np.arange(s0, min(s0 + chunk, nseed + 1), dtype=np.int32)
+        r, t = w.refl_trans_v1_batch(seeds)
+        if probatype == "incident":
+            tp, rp = np.abs(t[:, :, imu - 1]) ** 2, np.abs(r[:, :, imu - 1]) ** 2
+        else:
+            tp, rp = (np.abs(t) ** 2).sum(axis=1), (np.abs(r) ** 2).sum(axis=1)
+        for k in range(seeds.size):  # seed order, as the Fortran sum over dim=2
+            tsum += tp[k]
+            rsum += rp[k]
+    return tsum / nseed, rsum / nseed
+
+
+def task_tpattern(settings: dict, outdir: str = "out") -> str:
+    """task_tpattern (src/main.f90:735-838) for probatype 'incident' and
+    'total'; 'deposition' needs the full Green function inside the medium,
+    which this GPU build does not compute.  Returns the result file."""
+    tp = settings["tpattern"]
+    nseed, imode = int(tp.get("nseed", 0)), int(tp.get("imode", 1))
+    probatype = str(tp.get("probatype", "incident")).strip()
+    if nseed <= 0:
+        raise ValueError(f"Invalid number of disorder realizations (received {nseed}), aborting...")
+    if probatype not in ("incident", "total", "deposition"):
+        raise ValueError(f"Invalid probatype, received '{probatype}', expected incident/total/deposition, aborting...")
+    if probatype == "deposition":
+        raise ValueError("probatype 'deposition' needs the full Green function, which this GPU build does not "
+                         "compute, aborting...")
+    w = _waveguide_from(settings["waveguide"])
+    M = w.nmu
+    imu = (imode + M // 2 - 1) % M + 1 if w.get_parameters()["boundtype"] == "periodic" else imode
+    if not 1 <= imu <= M:
+        raise ValueError(f"Invalid incident mode imode={imode}, expected in [1, {M}], aborting...")
+    t0 = time.perf_counter()
+    tprob, rprob = tpattern_probabilities(w, nseed, imu, probatype)
+    tsec = time.perf_counter() - t0
+    ddir = os.path.join(generate_directory(w, outdir), "tpattern")
+    os.makedirs(ddir, exist_ok=True)
+    path = unique_filename(os.path.join(ddir, "result_"), ".csv")
+    pre = _preamble(w, nseed, 0, 1, tsec)[:4]  # timestamp and the waveguide parameters
+    with open(path, "w") as f:
+        for line in pre:
+            f.write(line + "\n")
+        f.write(f"%% Radiation pattern parameters: probatype='{probatype}', nseed={nseed}, imode={imode}, "
+                f"time={fortran_f(tsec, 3)} s.\n")
+        f.write("imu, tprob, rprob\n")
+        for i in range(M):
+            f.write(f"{i + 1}, {fortran_g0(tprob[i])}, {fortran_g0(rprob[i])}\n")
+    return path
+
+
 def plot_histo_from_file(settings: dict, datafile: str) -> str:
     """plot_histo_from_file (src/plot_histogram.f90:50-143): re-bin saved
     samples into replot_N.distrib.csv next to the data file."""
@@ -343,6 +402,8 @@ def main(argv=None) -> None:
     nml = read_namelists(open(a.settings).read())
     if a.replot:
         print(plot_histo_from_file(nml, a.datafile))
+    elif str(nml.get("settings", {}).get("task", "tdistrib")).strip() == "tpattern":
+        print(task_tpattern(nml, a.outdir))
     else:
         r = task_tdistrib(nml, a.outdir)
         print(r["distrib"], f"{r['time']:.3f} s")
