@@ -118,6 +118,68 @@ int rg_compute_refl_trans_v1(rg_waveguide* wg, int iseed, double* rmat, double* 
 int rg_refl_trans_v1_batch(rg_waveguide* wg, const int32_t* seeds, int n, double* rmat, double* tmat,
                            int32_t* status);
 
+/* ------------------------------------------------------------------------
+ * Full Green function (src/waveguide.f90:636-997).  The reference solves the
+ * whole block tridiagonal system (solve_block_tridiag,
+ * src/base_utils.f90:296-335) and keeps G(x_n; x_s) for every slice.  Here a
+ * forward sweep keeps each slice's (S_n, Z_n), and the backward pass runs
+ * only on the source vectors a result needs.  Positions are 1-based slice
+ * indices, as in the reference.
+ * ------------------------------------------------------------------------ */
+
+/* Profile kinds of rg_tprofile_batch:
+ *   RG_PROFILE_TPROFILE  compute_tprofile (src/waveguide.f90:843-907): the
+ *                        eigenvectors of t^H t (full nmu x nmu t) with
+ *                        a[w] <= T <= b[w], profile times 4/nt (nt != 0);
+ *   RG_PROFILE_ITX       compute_itx_profile (src/waveguide.f90:764-825): the
+ *                        same selection, times 2/(pi wol |b[w]-a[w]|);
+ *   RG_PROFILE_GROUP     compute_tprofile_group (src/waveguide.f90:924-997):
+ *                        t filtered to imin..imax x jmin..jmax, eigenvectors
+ *                        with |T - a[w]| <= b[w], times 4/nt (nt != 0). */
+#define RG_PROFILE_TPROFILE 0
+#define RG_PROFILE_ITX 1
+#define RG_PROFILE_GROUP 2
+
+/* Transmission-eigenstate profiles of n realizations: for seed seeds[k] and
+ * window w < nprofile, profiles[(k*nprofile + w)*nx + ix] (the reference's
+ * tprofiledata(nx, nprofile, nseed) layout), nt[k*nprofile + w] eigenvalues
+ * in the window and tavg[k] = sum(T)/ncol (the group's Tavg).  Host
+ * pointers; nt, tavg and status may be NULL.  The window bounds are checked
+ * as the reference checks them.  Returns the first non-OK status after all
+ * realizations have run. */
+int rg_tprofile_batch(rg_waveguide* wg, const int32_t* seeds, int n, int kind, int nprofile, const double* a,
+                      const double* b, double* profiles, int32_t* nt, double* tavg, int32_t* status);
+
+/* The reference's single-realization methods on top of it. */
+int rg_compute_tprofile(rg_waveguide* wg, int iseed, double tmin, double tmax, double* tprofile, int64_t len,
+                        int* nt);
+int rg_compute_itx_profile(rg_waveguide* wg, int iseed, double tmin, double tmax, double* itx, int64_t len);
+int rg_compute_tprofile_group(rg_waveguide* wg, int iseed, int nprofile, const double* tm, const double* dt,
+                              double* tprofile, int64_t len, int32_t* nt, double* tavg);
+
+/* compute_deposition (src/waveguide.f90:710-745): depmat = 2i sqrt(real(mu))
+ * G(x_fpos; x_ipos) sqrt(real(mu)), nmu x nmu complex, column-major (host). */
+int rg_compute_deposition(rg_waveguide* wg, int iseed, int fpos, int ipos, double* depmat);
+
+/* Deposition for n realizations (the deposition branch of the tpattern
+ * task, src/main.f90:802-806): col in 1..nmu gives column col of each
+ * realization's depmat (out + 2*k*nmu), col == 0 the whole matrix
+ * (out + 2*k*nmu*nmu).  Host pointers; status may be NULL. */
+int rg_deposition_batch(rg_waveguide* wg, const int32_t* seeds, int n, int fpos, int ipos, int col, double* out,
+                        int32_t* status);
+
+/* compute_wavefunction (src/waveguide.f90:636-698): the field of a unit
+ * source in mode imode at slice ipos, as the (nx*ny) x 5 table [x, y, Re psi,
+ * Im psi, upot] (host, column-major; rows = nx*ny). */
+int rg_compute_wavefunction(rg_waveguide* wg, int iseed, int ipos, int imode, double* wfundata, int64_t rows);
+
+/* diagonalize_ahca (src/base_utils.f90:394-444) on the GPU: the eigenvalues
+ * T[n] (descending) and eigenvectors U (n x n, column-major, same order) of
+ * A^H A for the m x n complex matrix a (column-major).  One-sided Jacobi with
+ * accumulated rotations instead of zgesvd; eigenvectors are defined up to a
+ * phase (and within degenerate eigenspaces). */
+int rg_diagonalize_ahca(const double* a, int m, int n, double* T, double* U);
+
 /* As rg_compute_tdistrib / rg_compute_refl_trans_v1, but for a caller-given
  * potential upot(nxdiso, ny) (host, column-major: x fastest), already scaled
  * by stdu as set_hamiltonian_waveguide stores it (src/waveguide.f90:366-372).

@@ -5,8 +5,9 @@
  * (src/waveguide.f90:13-73): the constructor is `init`, the copy constructor
  * `init_copy`, the destructor `del`, and the type-bound procedures keep their
  * names (get_nmu, get_neigv, get_nx, get_xmesh, get_parameters,
- * compute_tdistrib, compute_refl_trans_v1, print_parameters,
- * generate_directory).  Where the reference prints a message and stops
+ * compute_tdistrib, compute_refl_trans_v1, compute_wavefunction,
+ * compute_deposition, compute_itx_profile, compute_tprofile,
+ * compute_tprofile_group, print_parameters, generate_directory).  Where the reference prints a message and stops
  * (src/base_utils.f90:56-57), these methods throw recurgreen::Error carrying
  * the library's status code and message.  Header-only; link against
  * librecurgreen_gb300.so.
@@ -179,6 +180,63 @@ class Waveguide {
     check(rg_refl_trans_v1_batch(h_, seeds.data(), (int)seeds.size(),
                                  rmat ? reinterpret_cast<double*>(rmat->data()) : nullptr,
                                  reinterpret_cast<double*>(tmat.data()), nullptr));
+  }
+
+  // compute_tprofile (src/waveguide.f90:843-907): |psi_T(x)|^2 averaged over
+  // the transmission eigenstates with tmin <= T <= tmax; returns nt.
+  int compute_tprofile(int iseed, double tmin, double tmax, std::vector<double>& tprofile) {
+    tprofile.resize(get_nx());
+    int nt = 0;
+    check(rg_compute_tprofile(h_, iseed, tmin, tmax, tprofile.data(), (int64_t)tprofile.size(), &nt));
+    return nt;
+  }
+  // compute_itx_profile (src/waveguide.f90:764-825).
+  void compute_itx_profile(int iseed, double tmin, double tmax, std::vector<double>& itx) {
+    itx.resize(get_nx());
+    check(rg_compute_itx_profile(h_, iseed, tmin, tmax, itx.data(), (int64_t)itx.size()));
+  }
+  // compute_tprofile_group (src/waveguide.f90:924-997): tprofile is nx x
+  // nprofile, column-major (profile ip at ip*nx); returns Tavg.
+  double compute_tprofile_group(int iseed, const std::vector<double>& tm, const std::vector<double>& dt,
+                                std::vector<double>& tprofile, std::vector<int32_t>& nt) {
+    tprofile.resize((size_t)get_nx() * tm.size());
+    nt.resize(tm.size());
+    double tavg = 0.0;
+    if (tm.size() != dt.size()) throw Error(RG_ERR_INVALID_ARG, "tm and dt differ in length");
+    check(rg_compute_tprofile_group(h_, iseed, (int)tm.size(), tm.data(), dt.data(), tprofile.data(),
+                                    (int64_t)tprofile.size(), nt.data(), &tavg));
+    return tavg;
+  }
+  // The profiles of many seeds (kind RG_PROFILE_*): profiles[(k*nprofile + w)*nx + ix],
+  // nt[k*nprofile + w], tavg[k].
+  void tprofile_batch(const std::vector<int32_t>& seeds, int kind, const std::vector<double>& a,
+                      const std::vector<double>& b, std::vector<double>& profiles, std::vector<int32_t>& nt,
+                      std::vector<double>& tavg) {
+    if (a.size() != b.size()) throw Error(RG_ERR_INVALID_ARG, "window bounds differ in length");
+    profiles.resize(seeds.size() * a.size() * (size_t)get_nx());
+    nt.resize(seeds.size() * a.size());
+    tavg.resize(seeds.size());
+    check(rg_tprofile_batch(h_, seeds.data(), (int)seeds.size(), kind, (int)a.size(), a.data(), b.data(),
+                            profiles.data(), nt.data(), tavg.data(), nullptr));
+  }
+  // compute_deposition (src/waveguide.f90:710-745): nmu x nmu, column-major.
+  void compute_deposition(int iseed, int fpos, int ipos, std::vector<std::complex<double>>& depmat) {
+    depmat.resize((size_t)get_nmu() * get_nmu());
+    check(rg_compute_deposition(h_, iseed, fpos, ipos, reinterpret_cast<double*>(depmat.data())));
+  }
+  // Column col (1-based; 0: all) of the deposition matrix of many seeds.
+  void deposition_batch(const std::vector<int32_t>& seeds, int fpos, int ipos, int col,
+                        std::vector<std::complex<double>>& out) {
+    out.resize(seeds.size() * (size_t)get_nmu() * (col > 0 ? 1 : get_nmu()));
+    check(rg_deposition_batch(h_, seeds.data(), (int)seeds.size(), fpos, ipos, col,
+                              reinterpret_cast<double*>(out.data()), nullptr));
+  }
+  // compute_wavefunction (src/waveguide.f90:636-698): (nx*ny) x 5, column-major
+  // (columns x, y, Re psi, Im psi, upot).
+  void compute_wavefunction(int iseed, int ipos, int imode, std::vector<double>& wfundata) {
+    const int64_t rows = (int64_t)get_nx() * get_ny();
+    wfundata.resize(5 * (size_t)rows);
+    check(rg_compute_wavefunction(h_, iseed, ipos, imode, wfundata.data(), rows));
   }
 
   // print_parameters (src/waveguide.f90:1003-1018): three lines, each

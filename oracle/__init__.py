@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 import glob
+import math
 import os
 import subprocess
 
@@ -73,6 +74,11 @@ def lib() -> C.CDLL:
     L.orc_tdistrib_batch.argtypes = [vp, ip, C.c_int, dp, C.c_int]
     L.orc_histogram.argtypes = [dp, C.c_int64, dp, C.c_int, dp, dp]
     L.orc_prepare_distrib.argtypes = [dp, C.c_int64, C.c_int, dp, dp]
+    L.orc_diagonalize_ahca.argtypes = [vp, C.c_int, C.c_int, dp, vp]
+    L.orc_get_modal.argtypes = [vp, vp]
+    L.orc_get_meshes.argtypes = [vp, dp, dp]
+    L.orc_solve_block_tridiag.argtypes = [vp, dp, vp, C.c_int, vp]
+    L.orc_block_tridiag.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]
     path, prefix = _find_openblas()
     rc = L.orc_load_lapack(path.encode(), prefix.encode())
     if rc:
@@ -112,6 +118,7 @@ class Waveguide:
         for k in ("kdx", "dos", "stdu"):
             setattr(self, k, L.orc_get_real(h, k.encode()))
         self.nxdiso, self.nxfree = nxdiso, nxfree
+        self.wol, self.boundtype = wol, boundtype
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -156,6 +163,117 @@ class Waveguide:
         _check(lib().orc_refl_trans_v2_upot(self._h, _dp(upot), r.ctypes.data, t.ctypes.data))
         return r.T.copy(), t.T.copy()
 
+    # -- full Green function (src/waveguide.f90:636-997) --
+    def modal(self) -> np.ndarray:
+        m = np.zeros((self.nmu, self.ny), np.complex128)  # column-major (ny, nmu)
+        lib().orc_get_modal(self._h, m.ctypes.data)
+        return m.T.copy()
+
+    def meshes(self):
+        x = np.zeros(self.nx, np.float64)
+        y = np.zeros(self.ny, np.float64)
+        lib().orc_get_meshes(self._h, _dp(x), _dp(y))
+        return x, y
+
+    def solve_block_tridiag_upot(self, upot: np.ndarray, ind: np.ndarray) -> np.ndarray:
+        """solve_block_tridiag (src/base_utils.f90:296-335) on this guide's
+        blocks: ind and the result have shape (nx, nmu, k)."""
+        upot = np.ascontiguousarray(upot, np.float64)
+        nx, M, k = ind.shape
+        assert nx == self.nx and M == self.nmu
+        buf = np.ascontiguousarray(ind.transpose(0, 2, 1), np.complex128)  # column-major blocks
+        x = np.zeros_like(buf)
+        _check(lib().orc_solve_block_tridiag(self._h, _dp(upot), buf.ctypes.data, k, x.ctypes.data))
+        return x.transpose(0, 2, 1).copy()
+
+    def _green(self, upot, ipos: int, cols=None) -> np.ndarray:
+        """G(x_n; x_ipos) for all n: the identity source at block ipos (or
+        the unit vectors of the 0-based mode indices `cols`)."""
+        M = self.nmu
+        k = M if cols is None else len(cols)
+        ind = np.zeros((self.nx, M, k), np.complex128)
+        if cols is None:
+            ind[ipos - 1] = np.eye(M)
+        else:
+            for q, c in enumerate(cols):
+                ind[ipos - 1, c, q] = 1.0
+        return self.solve_block_tridiag_upot(upot, ind)
+
+    def _sqmu(self) -> np.ndarray:
+        return np.sqrt(self.tables()["mumesh"].real).astype(np.complex128)
+
+    def tprofile_upot(self, upot, tmin: float, tmax: float, itx: bool = False):
+        """compute_tprofile (src/waveguide.f90:843-907), or with itx
+        compute_itx_profile (src/waveguide.f90:764-825): (profile, nt)."""
+        green = self._green(upot, 1)
+        sq = self._sqmu()
+        tmat = 2.0j * (sq[:, None] * green[self.nx - 1] * sq[None, :])
+        tvals, U = diagonalize_ahca(tmat)
+        prof = np.zeros(self.nx, np.float64)
+        nt = 0
+        for iv in range(self.nmu):
+            if tmin <= tvals[iv] and tvals[iv] <= tmax:
+                for ix in range(self.nx):
+                    vec = green[ix] @ (sq * U[:, iv])
+                    prof[ix] = prof[ix] + np.sum((vec * vec.conj()).real)
+                nt += 1
+        if itx:
+            prof = prof * 2.0 / (math.pi * self.wol * abs(tmax - tmin))
+        elif nt != 0:
+            prof = prof * (4.0 / nt)
+        return prof, nt
+
+    def tprofile_group_upot(self, upot, tm, dt):
+        """compute_tprofile_group (src/waveguide.f90:924-997): (tprofile
+        (nx, nprofile), nt (nprofile,), tavg)."""
+        green = self._green(upot, 1)
+        sq = self._sqmu()
+        i0, i1, j0, j1 = self.imin - 1, self.imax, self.jmin - 1, self.jmax
+        tmat = 2.0j * (sq[i0:i1, None] * green[self.nx - 1][i0:i1, j0:j1] * sq[None, j0:j1])
+        if self.neigv != j1 - j0:
+            raise OracleError(1, "zgesvd: Invalid number of singular values")
+        tvals, U = diagonalize_ahca(tmat)
+        tavg = np.sum(tvals) / self.neigv
+        npf = len(tm)
+        prof = np.zeros((self.nx, npf), np.float64)
+        nt = np.zeros(npf, np.int32)
+        for ip in range(npf):
+            for iv in range(self.neigv):
+                if abs(tvals[iv] - tm[ip]) <= dt[ip]:
+                    for ix in range(self.nx):
+                        vec = green[ix][:, j0:j1] @ (sq[j0:j1] * U[:, iv])
+                        prof[ix, ip] = prof[ix, ip] + np.sum((vec * vec.conj()).real)
+                    nt[ip] += 1
+            if nt[ip] != 0:
+                prof[:, ip] = prof[:, ip] * (4.0 / nt[ip])
+        return prof, nt, tavg
+
+    def deposition_upot(self, upot, fpos: int, ipos: int) -> np.ndarray:
+        """compute_deposition (src/waveguide.f90:710-745): depmat (nmu, nmu)."""
+        green = self._green(upot, ipos)
+        sq = self._sqmu()
+        return 2.0j * (sq[:, None] * green[fpos - 1] * sq[None, :])
+
+    def wavefunction_upot(self, upot, ipos: int, imode: int) -> np.ndarray:
+        """compute_wavefunction (src/waveguide.f90:636-698): (nx*ny, 5)."""
+        M = self.nmu
+        imu = (imode + M // 2 - 1) % M + 1 if self.boundtype == "periodic" else imode
+        green = self._green(upot, ipos, cols=[imu - 1])
+        modal = self.modal()
+        x, y = self.meshes()
+        out = np.zeros((self.nx * self.ny, 5), np.float64)
+        for ix in range(self.nx):
+            psi = modal @ green[ix, :, 0]
+            rows = slice(ix * self.ny, (ix + 1) * self.ny)
+            out[rows, 0] = x[ix]
+            out[rows, 1] = y
+            out[rows, 2] = psi.real
+            out[rows, 3] = psi.imag
+        u = np.asarray(upot)
+        for ix in range(self.nxdiso):
+            out[(ix + self.nxfree) * self.ny:(ix + self.nxfree + 1) * self.ny, 4] = u[:, ix]
+        return out
+
     def compute_tdistrib(self, iseed: int, tallvals: np.ndarray) -> None:
         assert tallvals.dtype == np.float64 and tallvals.flags.c_contiguous
         _check(lib().orc_compute_tdistrib(self._h, iseed, _dp(tallvals), tallvals.size))
@@ -194,6 +312,29 @@ def singular_values(a: np.ndarray) -> np.ndarray:
     s = np.zeros(min(m, n), np.float64)
     _check(lib().orc_singular_values(f.ctypes.data, m, n, _dp(s)))
     return s
+
+
+def block_tridiag(amat: np.ndarray, bdiag: np.ndarray, imat: np.ndarray) -> np.ndarray:
+    """solve_block_tridiag, src/base_utils.f90:296-335: amat (nb, m, m),
+    bdiag (m,), imat (nb, m, k) -> xmat (nb, m, k)."""
+    nb, m, _ = amat.shape
+    k = imat.shape[2]
+    a = np.ascontiguousarray(np.asarray(amat, np.complex128).transpose(0, 2, 1))
+    b = np.ascontiguousarray(bdiag, np.complex128)
+    i = np.ascontiguousarray(np.asarray(imat, np.complex128).transpose(0, 2, 1))
+    x = np.zeros_like(i)
+    _check(lib().orc_block_tridiag(a.ctypes.data, b.ctypes.data, i.ctypes.data, nb, m, k, x.ctypes.data))
+    return x.transpose(0, 2, 1).copy()
+
+
+def diagonalize_ahca(a: np.ndarray):
+    """diagonalize_ahca, src/base_utils.f90:394-444 (zgesvd 'N','A'): (T, U)."""
+    f = np.asfortranarray(a, np.complex128).copy(order="F")
+    m, n = f.shape
+    T = np.zeros(n, np.float64)
+    U = np.zeros((n, n), np.complex128, order="F")
+    _check(lib().orc_diagonalize_ahca(f.ctypes.data, m, n, _dp(T), U.ctypes.data))
+    return T, U
 
 
 def histogram(samples, bins):

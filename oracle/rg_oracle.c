@@ -370,6 +370,49 @@ int orc_singular_values(cplx* a, int m, int n, double* s) {
   return ORC_OK;
 }
 
+/* diagonalize_ahca, src/base_utils.f90:394-444: zgesvd('N','A') of the m x n
+ * matrix a (destroyed); T (n entries, the first min(m,n) written, the rest
+ * zero here) receives the squared singular values in descending order and U
+ * (n x n, column-major) = (W^H)^H, the eigenvectors of A^H A. */
+int orc_diagonalize_ahca(cplx* a, int m, int n, double* T, cplx* U) {
+  if (need_lapack()) return ORC_ERR_LAPACK;
+  const int mn = m < n ? m : n;
+  int lwork = 2 * mn + (m > n ? m : n);
+  if (lwork < 1) lwork = 1;
+  cplx* work = (cplx*)malloc(sizeof(cplx) * lwork);
+  double* rwork = (double*)malloc(sizeof(double) * 5 * (mn > 0 ? mn : 1));
+  cplx* wh = (cplx*)malloc(sizeof(cplx) * (size_t)n * n);
+  cplx v[1];
+  int info = 0, ldv = m, ldwh = n;
+  for (int k = 0; k < n; ++k) T[k] = 0.0;
+  p_zgesvd("N", "A", &m, &n, a, &m, T, v, &ldv, wh, &ldwh, work, &lwork, rwork, &info, 1, 1);
+  if (info == 0) {
+    for (int k = 0; k < n; ++k) T[k] = T[k] * T[k];
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) U[i + (size_t)n * j] = conj(wh[j + (size_t)n * i]);
+  }
+  free(work);
+  free(rwork);
+  free(wh);
+  if (info != 0) {
+    snprintf(g_err, sizeof g_err, "zgesvd failed (LAPACK info=%d)", info);
+    return ORC_ERR_LAPACK;
+  }
+  return ORC_OK;
+}
+
+/* The modal matrix modal(iy, imu) (ny x nmu, column-major),
+ * src/waveguide.f90:179-185 and :221-227. */
+void orc_get_modal(const orc_wg* w, cplx* modal) {
+  memcpy(modal, w->modal, sizeof(cplx) * (size_t)w->ny * w->nmu);
+}
+
+/* xmesh (nx) and ymesh (ny), src/waveguide.f90:145-146 and :172,212. */
+void orc_get_meshes(const orc_wg* w, double* xmesh, double* ymesh) {
+  if (xmesh) memcpy(xmesh, w->xmesh, sizeof(double) * w->nx);
+  if (ymesh) memcpy(ymesh, w->ymesh, sizeof(double) * w->ny);
+}
+
 /* C = alpha * op(A) * B via zgemm (the reference uses gfortran's intrinsic
  * matmul, src/waveguide.f90:379,438; any FP64 summation order is equally
  * valid). */
@@ -550,6 +593,65 @@ int orc_refl_trans_v2_upot(const orc_wg* w, const double* upot, cplx* rmat, cplx
     }
 done:
   free(smat); free(zmat); free(x); free(tmp); free(work);
+  return rc;
+}
+
+/* solve_block_tridiag, src/base_utils.f90:296-335: nb diagonal blocks amat
+ * (nmu x nmu each), the diagonal bdiag of B, the independent term `ind` and
+ * the solution `x` (nb blocks of nmu x k); every block column-major, block i
+ * at offset i*nmu*nmu (amat) or i*nmu*k (ind, x).  Forward loop
+ * S_1 = inv(A_1), Z_1 = S_1 I_1; S_i = inv(A_i - B S_{i-1} B),
+ * Z_i = S_i (I_i - B Z_{i-1}); backward loop X_n = Z_n,
+ * X_i = Z_i - S_i (B X_{i+1}). */
+int orc_block_tridiag(const cplx* amat, const cplx* bdiag, const cplx* ind, int nb, int nmu, int k, cplx* x) {
+  const size_t mm = (size_t)nmu * nmu, mk = (size_t)nmu * k;
+  if (need_lapack()) return ORC_ERR_LAPACK;
+  if (k < 1 || nb < 1 || nmu < 1) { snprintf(g_err, sizeof g_err, "solve_block_tridiag: empty system"); return ORC_ERR_ARG; }
+  cplx* smat = (cplx*)malloc(sizeof(cplx) * mm * nb);
+  cplx* zmat = (cplx*)malloc(sizeof(cplx) * mk * nb);
+  cplx* tmp = (cplx*)malloc(sizeof(cplx) * mk);
+  int rc = ORC_OK;
+  memcpy(smat, amat, sizeof(cplx) * mm);
+  if ((rc = orc_inverse_complex(smat, nmu))) goto done;
+  gemm("N", nmu, k, nmu, 1.0, smat, nmu, ind, nmu, zmat, nmu);
+  for (int i = 1; i < nb; ++i) {
+    cplx* si = smat + mm * i;
+    const cplx* sp = smat + mm * (i - 1);
+    const cplx* ai = amat + mm * i;
+    for (int c = 0; c < nmu; ++c)
+      for (int a = 0; a < nmu; ++a)
+        si[a + (size_t)nmu * c] = ai[a + (size_t)nmu * c] - (bdiag[a] * sp[a + (size_t)nmu * c]) * bdiag[c];
+    if ((rc = orc_inverse_complex(si, nmu))) goto done;
+    const cplx* zp = zmat + mk * (i - 1);
+    const cplx* ii = ind + mk * i;
+    for (int c = 0; c < k; ++c)
+      for (int a = 0; a < nmu; ++a) tmp[a + (size_t)nmu * c] = ii[a + (size_t)nmu * c] - bdiag[a] * zp[a + (size_t)nmu * c];
+    gemm("N", nmu, k, nmu, 1.0, si, nmu, tmp, nmu, zmat + mk * i, nmu);
+  }
+  memcpy(x + mk * (nb - 1), zmat + mk * (nb - 1), sizeof(cplx) * mk);
+  for (int i = nb - 2; i >= 0; --i) {
+    const cplx* xn = x + mk * (i + 1);
+    for (int c = 0; c < k; ++c)
+      for (int a = 0; a < nmu; ++a) tmp[a + (size_t)nmu * c] = bdiag[a] * xn[a + (size_t)nmu * c];
+    cplx* xi = x + mk * i;
+    gemm("N", nmu, k, nmu, 1.0, smat + mm * i, nmu, tmp, nmu, xi, nmu);
+    for (size_t e = 0; e < mk; ++e) xi[e] = zmat[mk * i + e] - xi[e];
+  }
+done:
+  free(smat); free(zmat); free(tmp);
+  return rc;
+}
+
+/* solve_block_tridiag on the waveguide's blocks: amat of
+ * set_hamiltonian_waveguide (src/waveguide.f90:349-384) for potential upot,
+ * B = bmat, independent term `ind` of nx blocks nmu x k. */
+int orc_solve_block_tridiag(const orc_wg* w, const double* upot, const cplx* ind, int k, cplx* x) {
+  const size_t mm = (size_t)w->nmu * w->nmu;
+  cplx* amat = (cplx*)malloc(sizeof(cplx) * mm * w->nx);
+  cplx* work = (cplx*)malloc(sizeof(cplx) * ((size_t)w->ny * w->nmu + mm));
+  for (int i = 0; i < w->nx; ++i) slice_matrix(w, upot, i, amat + mm * i, work);
+  const int rc = orc_block_tridiag(amat, w->bmat, ind, w->nx, w->nmu, k, x);
+  free(amat); free(work);
   return rc;
 }
 

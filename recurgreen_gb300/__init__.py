@@ -28,7 +28,10 @@ EXPORTS = (
     "rg_potential", "rg_tdistrib_batch", "rg_tdistrib_batch_device", "rg_histogram",
     "rg_tdistrib_seed_noalloc", "rg_last_sweep_time", "rg_tdistrib_multi", "rg_sweep_segment",
     "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info", "rg_refl_trans_v1_batch",
+    "rg_tprofile_batch", "rg_compute_tprofile", "rg_compute_itx_profile", "rg_compute_tprofile_group",
+    "rg_compute_deposition", "rg_deposition_batch", "rg_compute_wavefunction", "rg_diagonalize_ahca",
 )
+PROFILE_KINDS = {"tprofile": 0, "itx": 1, "group": 2}
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
 
 
@@ -86,6 +89,14 @@ def lib() -> C.CDLL:
     L.rg_get_modes.argtypes = [vp, vp, vp]
     L.rg_last_batch_info.argtypes = [vp, C.POINTER(rg_batch_info)]
     L.rg_refl_trans_v1_batch.argtypes = [vp, ip, C.c_int, vp, vp, ip]
+    L.rg_tprofile_batch.argtypes = [vp, ip, C.c_int, C.c_int, C.c_int, dp, dp, dp, ip, dp, ip]
+    L.rg_compute_tprofile.argtypes = [vp, C.c_int, C.c_double, C.c_double, dp, i64, C.POINTER(C.c_int)]
+    L.rg_compute_itx_profile.argtypes = [vp, C.c_int, C.c_double, C.c_double, dp, i64]
+    L.rg_compute_tprofile_group.argtypes = [vp, C.c_int, C.c_int, dp, dp, dp, i64, ip, dp]
+    L.rg_compute_deposition.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+    L.rg_deposition_batch.argtypes = [vp, ip, C.c_int, C.c_int, C.c_int, C.c_int, vp, ip]
+    L.rg_compute_wavefunction.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, i64]
+    L.rg_diagonalize_ahca.argtypes = [vp, C.c_int, C.c_int, dp, vp]
     _LIB = L
     return L
 
@@ -250,6 +261,85 @@ class Waveguide:
         _check(rc)
         return out
 
+    # -- full Green function (src/waveguide.f90:636-997) --
+    def tprofile_batch(self, seeds, kind: str, a, b, return_status: bool = False):
+        """Transmission-eigenstate profiles of many seeds.  kind "tprofile"
+        (windows a[w] <= T <= b[w], full t, times 4/nt), "itx" (same windows,
+        times 2/(pi wol |b-a|)) or "group" (|T - a[w]| <= b[w], filtered t,
+        times 4/nt).  Returns (profiles (n, nprofile, nx), nt (n, nprofile),
+        tavg (n,)) [and the status array]."""
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        a = np.ascontiguousarray(np.atleast_1d(a), np.float64)
+        b = np.ascontiguousarray(np.atleast_1d(b), np.float64)
+        if a.shape != b.shape:
+            raise RecurGreenError(RG_ERR_INVALID_ARG, "window bounds must have the same length")
+        n, npf = seeds.size, a.size
+        prof = np.zeros((n, npf, self.nx), np.float64)
+        nt = np.zeros((n, npf), np.int32)
+        tavg = np.zeros(n, np.float64)
+        st = np.zeros(n, np.int32)
+        ip = C.POINTER(C.c_int32)
+        rc = lib().rg_tprofile_batch(self._h, seeds.ctypes.data_as(ip), n, PROFILE_KINDS.get(kind, -1), npf, _dp(a),
+                                     _dp(b), _dp(prof), nt.ctypes.data_as(ip), _dp(tavg), st.ctypes.data_as(ip))
+        if return_status:
+            return prof, nt, tavg, st
+        _check(rc)
+        return prof, nt, tavg
+
+    def compute_tprofile(self, iseed: int, tmin: float, tmax: float):
+        """compute_tprofile (src/waveguide.f90:843-907) -> (tprofile (nx,), nt)."""
+        out = np.zeros(self.nx, np.float64)
+        nt = C.c_int()
+        _check(lib().rg_compute_tprofile(self._h, int(iseed), tmin, tmax, _dp(out), out.size, C.byref(nt)))
+        return out, nt.value
+
+    def compute_itx_profile(self, iseed: int, tmin: float, tmax: float) -> np.ndarray:
+        """compute_itx_profile (src/waveguide.f90:764-825) -> itx (nx,)."""
+        out = np.zeros(self.nx, np.float64)
+        _check(lib().rg_compute_itx_profile(self._h, int(iseed), tmin, tmax, _dp(out), out.size))
+        return out
+
+    def compute_tprofile_group(self, iseed: int, tm, dt):
+        """compute_tprofile_group (src/waveguide.f90:924-997) -> (tprofile
+        (nx, nprofile), nt (nprofile,), tavg)."""
+        tm = np.ascontiguousarray(tm, np.float64)
+        dt = np.ascontiguousarray(dt, np.float64)
+        out = np.zeros((tm.size, self.nx), np.float64)  # Fortran (nx, nprofile) memory order
+        nt = np.zeros(tm.size, np.int32)
+        tavg = C.c_double()
+        _check(lib().rg_compute_tprofile_group(self._h, int(iseed), tm.size, _dp(tm), _dp(dt), _dp(out), out.size,
+                                               nt.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(tavg)))
+        return out.T.copy(), nt, tavg.value
+
+    def compute_deposition(self, iseed: int, fpos: int, ipos: int) -> np.ndarray:
+        """compute_deposition (src/waveguide.f90:710-745) -> depmat (nmu, nmu)."""
+        d = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_compute_deposition(self._h, int(iseed), int(fpos), int(ipos), d.ctypes.data))
+        return d
+
+    def deposition_batch(self, seeds, fpos: int, ipos: int, col: int = 0, return_status: bool = False):
+        """Deposition matrices of many seeds: (n, nmu, nmu), or column col
+        (1-based) of each, (n, nmu)."""
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        n, M = seeds.size, self.nmu
+        out = np.zeros((n, M) if col else (n, M, M), np.complex128)
+        st = np.zeros(n, np.int32)
+        ip = C.POINTER(C.c_int32)
+        rc = lib().rg_deposition_batch(self._h, seeds.ctypes.data_as(ip), n, int(fpos), int(ipos), int(col),
+                                       out.ctypes.data, st.ctypes.data_as(ip))
+        res = out if col else out.transpose(0, 2, 1)
+        if return_status:
+            return res, st
+        _check(rc)
+        return res
+
+    def compute_wavefunction(self, iseed: int, ipos: int, imode: int) -> np.ndarray:
+        """compute_wavefunction (src/waveguide.f90:636-698) -> wfundata
+        (nx*ny, 5): columns x, y, Re psi, Im psi, upot."""
+        rows = self.nx * self.ny
+        out = np.zeros((5, rows), np.float64)  # column-major (rows, 5)
+        _check(lib().rg_compute_wavefunction(self._h, int(iseed), int(ipos), int(imode), _dp(out), rows))
+        return out.T.copy()
 
     def last_batch_info(self) -> dict:
         """Kernel, grid, cluster and pivoted re-runs of the last tdistrib_batch."""
@@ -283,6 +373,17 @@ def tdistrib_multi(items, return_status: bool = False):
         return res, st
     _check(rc)
     return res
+
+
+def diagonalize_ahca(a):
+    """diagonalize_ahca (src/base_utils.f90:394-444) on the GPU: (T, U) with
+    A^H A = U diag(T) U^H, T descending."""
+    a = np.asfortranarray(a, np.complex128)
+    m, n = a.shape
+    T = np.zeros(n, np.float64)
+    U = np.zeros((n, n), np.complex128, order="F")
+    _check(lib().rg_diagonalize_ahca(a.ctypes.data, m, n, _dp(T), U.ctypes.data))
+    return T, U
 
 
 def histogram(samples, bins):

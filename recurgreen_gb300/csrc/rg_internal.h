@@ -89,6 +89,11 @@ struct SweepArgs {
   const int* count_ptr;       // device-side queue length; nullptr: nreal
   int force_cluster;          // > 0: cluster size for the blocked kernels instead of the heuristic
                               // (autotuner, multi calls with long items)
+  // Source slice of the Green-function column (pivoted blocked kernel, fresh
+  // start): Gs1 after slice n is Z_n of solve_block_tridiag for the identity
+  // source at slice inject_at (src/base_utils.f90:318-324), zero before it.
+  // 0 is the usual sweep (source at slice 0, where Z_0 = Gss_0).
+  int inject_at;
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were
@@ -152,5 +157,113 @@ struct NoAllocView {
   double sym_tau;  // SweepArgs::sym_tau
 };
 int noalloc_view(const rg_waveguide* w, NoAllocView* out);
+
+// ---------------------------------------------------------------------------
+// Full Green-function column (rg_green.cu, rg_green.cpp): the block
+// tridiagonal solve of src/base_utils.f90:296-335 for a source at one slice,
+// as a forward sweep that keeps (Gss_n, Gs1_n) = (S_n, Z_n) of every slice
+// and a back-substitution X_n = Z_n - S_n B X_{n+1} applied to a few source
+// vectors.
+// ---------------------------------------------------------------------------
+
+// What rg_green.cpp needs of a handle.
+struct GreenView {
+  int device, sm_count;
+  cudaStream_t stream;
+  const WgDesc* d_desc;
+  WgDesc desc;      // host copy: sizes and device table pointers
+  int* d_counter;   // kQueueCounters ints
+  int nxdiso, nxfree, nx, ny, nmu, neigv, periodic;
+  int imin, imax, jmin, jmax;  // 1-based Fisher-Lee window
+  double wol, stdu;
+  const double* xmesh;   // host [nx]
+  const double* ymesh;   // host [ny]
+  const double* kpmesh;  // host [nmu]
+  const cplx* sqmu_r;    // host [nmu] sqrt(real(mu))
+};
+int green_view(const rg_waveguide* w, GreenView* out);
+
+// Eigenvectors of t^H t per item (diagonalize_ahca, src/base_utils.f90:394-444)
+// and, for the transmission-eigenstate profiles, the selection of the
+// eigenvectors inside windows of T and their source vectors.
+struct EigvecArgs {
+  int nreal;
+  const double2* a;     // item r's matrix at a + r*astride, column-major with leading dimension lda
+  int64_t astride;
+  int lda;
+  int row0, nr, col0, nc;  // the block of a that is diagonalized (nr x nc)
+  double2* work;        // per-item workspace, work_stride double2: the block and V
+  int64_t work_stride;
+  double* tvals;        // [nreal][nc] eigenvalues, descending (ties by index)
+  double2* u;           // optional [nreal][nc][nc] eigenvectors, column-major, in tvals order
+  // Selection (when wsel != nullptr): eigenvector v enters window w when
+  //   centered == 0: wa[w] <= T_v <= wb[w]   (compute_tprofile, src/waveguide.f90:892)
+  //   centered == 1: |T_v - wa[w]| <= wb[w]  (compute_tprofile_group, src/waveguide.f90:978)
+  int nprof, centered;
+  const double* wa;     // [nprof]
+  const double* wb;     // [nprof]
+  int M;                // length of a source vector
+  const double2* sqmu;  // [M] sqrt(real(mu)); source row col0 + j is sqmu[col0 + j] * V[j][v]
+  double2* wsel;        // [nreal][nc][M] source vectors of the selected eigenvectors, in tvals order
+  uint32_t* member;     // [nreal][nc] bit w: in window w
+  int32_t* ksel;        // [nreal] selected count
+  int32_t* nt;          // [nreal][nprof] eigenvalues in each window
+  double* tavg;         // optional [nreal] sum(tvals) / nc
+  int32_t* status;      // [nreal]
+};
+int launch_eigvec(const EigvecArgs& a, cudaStream_t s);
+int64_t eigvec_work_stride(int nr, int nc);
+
+// Back-substitution over slices nx-1 .. i_lo for the source vectors of each
+// item: Y_{nx-1} = Z_{nx-1} W, Y_n = Z_n W - S_n (B Y_{n+1}).
+constexpr int kBackProfile = 0;  // prof[r][s][n] = sum_m |Y_n[m][s]|^2
+constexpr int kBackColumns = 1;  // cols[r][n - i_lo][s][m] = Y_n[m][s] (or only n = i_lo)
+struct BackArgs {
+  int nreal, M, nx;
+  const double2* dump;     // [nreal][nx][2][M][M]: (Gss_n, Gs1_n), row-major
+  const double2* bmat;     // [M]
+  const double2* src;      // item r's source vectors at src + r*src_stride, [kmax][M]
+  int64_t src_stride;      // 0: every item uses the same vectors
+  int kmax;
+  const int32_t* kcount;   // [nreal] vectors per item; nullptr: kmax
+  int i_lo;                // lowest slice, 0-based
+  int out_mode;            // kBackProfile or kBackColumns
+  int only_lo;             // kBackColumns: write slice i_lo only
+  const double2* left;     // kBackColumns, optional: output 2i * left[m] * Y[m][s] (Fisher-Lee rows)
+  double* prof;            // [nreal][kmax][nx]
+  double2* cols;           // [nreal][nslices][kmax][M], nslices = only_lo ? 1 : nx - i_lo
+};
+int launch_back(const BackArgs& a, cudaStream_t s);
+
+// Window sums of the per-vector profiles, normalised: out[r][w][n] =
+//   sum over selected s in window w (ascending s) of prof[r][s][n], times
+//   4/nt[r][w] when nt != 0 (compute_tprofile[_group], src/waveguide.f90:902,988), or
+//   2/(pi wol |wb[w] - wa[w]|) for kind RG_PROFILE_ITX (src/waveguide.f90:821).
+struct WindowArgs {
+  int nreal, nx, kmax, nprof, kind;
+  double wol;
+  const double* wa;        // [nprof]
+  const double* wb;        // [nprof]
+  const int32_t* ksel;
+  const uint32_t* member;
+  const int32_t* nt;
+  const double* prof;
+  double* out;             // [nreal][nprof][nx]
+};
+int launch_windows(const WindowArgs& a, cudaStream_t s);
+
+// compute_wavefunction's pixels (src/waveguide.f90:680-695): psi(x_n, y_j) =
+// sum_m modal[j][m] Y_n[m], written with x, y and the potential as the
+// (nx*ny) x 5 column-major table [x, y, Re psi, Im psi, upot].
+struct WavefunArgs {
+  int nx, ny, M, nxfree, nxdiso;
+  const double2* y;        // [nx][M]
+  const double2* modal;    // [ny][M]
+  const double* xmesh;     // [nx]
+  const double* ymesh;     // [ny]
+  const double* upot;      // [nxdiso][ny] (x-major rows of ny)
+  double* out;             // [5][nx*ny]
+};
+int launch_wavefun(const WavefunArgs& a, cudaStream_t s);
 
 }  // namespace rg

@@ -132,7 +132,9 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         colmap[c] = c;
       }
     } else {
-      for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+      // Source at slice 0: R = I.  A later source slice starts from R = 0.
+      const double one = a.inject_at > 0 ? 0.0 : 1.0;
+      for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? one : 0.0, 0.0);
     }
     if (draw) {
       for (int iy = ctid; iy < ny; iy += CNT) {
@@ -205,6 +207,10 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
       cur ^= 1;
       const double2* adiag = (n == 0 || n == wd.nx - 1) ? wd.adiag_edge : wd.adiag_bulk;
       const double rsign = (n == 1) ? 1.0 : -1.0;
+      // At the source slice s > 0 the right-hand side is the identity source:
+      // Z_s = S_s I, and the stored R carries Gs1 = -R, so R's right-hand
+      // side is -I in the physical rows (row q of W is physical row pinv[q]).
+      const bool source = (n > 0 && n == a.inject_at);
       for (int64_t e = ctid; e < mm; e += CNT) {
         const int q = (int)(e / M), c = (int)(e % M);
         const int al = (n == 0) ? q : pinv[q];
@@ -222,7 +228,8 @@ __global__ void __launch_bounds__(kLargeNT, 2) sweep_large_kernel(SweepArgs a) {
         }
         if (n > 0) {
           x = csub(x, cmul(cmul(wd.bmat[al], __ldcg(Wold + (int64_t)q * M + colmap[c])), wd.bmat[c]));
-          Rg[e] = cmul(wd.bmat[al], cscale(rsign, __ldcg(Rg + e)));
+          Rg[e] = source ? make_double2(al == c ? -1.0 : 0.0, 0.0)
+                         : cmul(wd.bmat[al], cscale(rsign, __ldcg(Rg + e)));
         }
         W[e] = x;
       }

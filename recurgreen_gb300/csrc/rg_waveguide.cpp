@@ -792,6 +792,34 @@ int noalloc_view(const rg_waveguide* w, NoAllocView* out) {
   return RG_OK;
 }
 
+int green_view(const rg_waveguide* w, GreenView* out) {
+  if (!w || !out) return fail(RG_ERR_INVALID_ARG, "green_view: NULL argument");
+  out->device = w->device;
+  out->sm_count = w->sm_count;
+  out->stream = w->stream;
+  out->d_desc = w->d_desc;
+  out->desc = w->h_desc;
+  out->d_counter = w->d_counter;
+  out->nxdiso = w->p.nxdiso;
+  out->nxfree = w->p.nxfree;
+  out->nx = w->nx;
+  out->ny = w->ny;
+  out->nmu = w->nmu;
+  out->neigv = w->neigv;
+  out->periodic = w->p.boundtype == RG_BOUND_PERIODIC;
+  out->imin = w->imin;
+  out->imax = w->imax;
+  out->jmin = w->jmin;
+  out->jmax = w->jmax;
+  out->wol = w->p.wol;
+  out->stdu = w->stdu;
+  out->xmesh = w->xmesh.data();
+  out->ymesh = w->ymesh.data();
+  out->kpmesh = w->kpmesh.data();
+  out->sqmu_r = w->sqmu_r.data();
+  return RG_OK;
+}
+
 }  // namespace rg
 
 // ---------------------------------------------------------------------------

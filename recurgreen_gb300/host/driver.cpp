@@ -317,6 +317,19 @@ bool nml_logical(const NmlGroup& g, const std::string& key, bool def) {
   invalid_entry(v->line);
 }
 
+std::vector<double> nml_reals(const NmlGroup& g, const std::string& key, size_t n, const std::vector<double>& def) {
+  const NmlValue* v = find(g, key);
+  if (!v) return def;
+  std::vector<double> out;
+  for (const std::string& it : v->items) {
+    double x = 0.0;
+    if (!parse_real(it, &x)) invalid_entry(v->line);
+    out.push_back(x);
+  }
+  if (out.size() != n) invalid_entry(v->line);
+  return out;
+}
+
 std::string format_g0(double x, int d) {
   if (std::isnan(x)) return "NaN";
   if (std::isinf(x)) return x > 0 ? "Infinity" : "-Infinity";
@@ -491,8 +504,190 @@ void task_tdistrib(const std::string& text, const std::string& root) {
   }
 }
 
-// task_tpattern (src/main.f90:735-877) for probatype 'incident' and 'total':
-// the mean over seeds of |t_{b,imu}|^2, |r_{b,imu}|^2 or of their column sums.
+// print_timestamp + print_parameters (src/base_utils.f90:722-739,
+// src/waveguide.f90:1003-1018).
+void write_header(std::FILE* fp, const recurgreen::Waveguide& w) {
+  std::fprintf(fp, "%%%% Computed on %s by %s\n", timestamp().c_str(), kProgram);
+  w.print_parameters(fp, "%%");
+}
+
+// save_real_matrix (src/base_utils.f90:639-657) with 'g0.16' and ', ': the
+// nrow x ncol matrix a(i, j) = at(i, j), one row per line.
+template <class F>
+void write_matrix(std::FILE* fp, size_t nrow, size_t ncol, F at) {
+  for (size_t i = 0; i < nrow; ++i) {
+    for (size_t j = 0; j < ncol; ++j)
+      std::fprintf(fp, "%s%s", format_g0(at(i, j)).c_str(), j + 1 < ncol ? ", " : "\n");
+  }
+}
+
+std::FILE* open_output(const std::string& fname) {
+  std::FILE* fp = std::fopen(fname.c_str(), "w");
+  if (!fp) throw Stop("Cannot open file: " + fname);
+  return fp;
+}
+
+double seconds_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+std::vector<int32_t> seeds_1_to(long nseed) {
+  std::vector<int32_t> seeds(nseed);
+  for (long k = 0; k < nseed; ++k) seeds[k] = (int32_t)(k + 1);
+  return seeds;
+}
+
+// task_wavefunction and save_wavefunction (src/main.f90:335-398).
+void task_wavefunction(const std::string& text, const std::string& root) {
+  const recurgreen::Parameters p = waveguide_parameters(text);
+  const NmlGroup wf = read_namelist(text, "wavefunction", {"iseed", "ipos", "imode"});
+  const long iseed = nml_int(wf, "iseed", 1), ipos = nml_int(wf, "ipos", 1), imode = nml_int(wf, "imode", 1);
+  recurgreen::Waveguide w(p);
+  w.print_parameters(stdout, strip(tag_info()));
+  std::printf("%sWavefunction parameters: iseed=%ld, ipos=%ld, imode=%ld\n", tag_info().c_str(), iseed, ipos, imode);
+  std::vector<double> data;
+  w.compute_wavefunction((int)iseed, (int)ipos, (int)imode, data);
+  std::printf("%sSaving the wavefunction to a CSV file...\n", tag_info().c_str());
+  const std::string dir = w.generate_directory(root) + "wavefun/";
+  create_directory(dir);
+  const std::string fname = unique_filename(dir + "result_", ".wavefun.csv");
+  std::FILE* fp = open_output(fname);
+  write_header(fp, w);
+  std::fprintf(fp, "%%%% Wavefunction parameters: iseed=%ld, ipos=%ld, imode=%ld\n", iseed, ipos, imode);
+  std::fprintf(fp, "x, y, repsi, impsi, upot\n");
+  const size_t rows = data.size() / 5;
+  write_matrix(fp, rows, 5, [&](size_t i, size_t j) { return data[j * rows + i]; });
+  std::fclose(fp);
+  std::printf("%sResult written in file: %s\n", tag_info().c_str(), fname.c_str());
+}
+
+// task_tprofile and save_tprofile (src/main.f90:405-565).
+void task_tprofile(const std::string& text, const std::string& root) {
+  const recurgreen::Parameters p = waveguide_parameters(text);
+  const NmlGroup tp = read_namelist(text, "tprofile", {"tmin", "tmax", "nseed", "nthreads"});
+  const double tmin = nml_real(tp, "tmin", 0.0), tmax = nml_real(tp, "tmax", 1.0);
+  const long nseed = nml_int(tp, "nseed", 0);
+  recurgreen::Waveguide w(p);
+  w.print_parameters(stdout, strip(tag_info()));
+  if (nseed <= 0)
+    throw Stop("Invalid number of disorder realizations (received " + fmt_int(nseed) + "), aborting...");
+  const int nx = w.get_nx();
+  std::vector<double> prof, tavg;
+  std::vector<int32_t> nt;
+  const auto t0 = std::chrono::steady_clock::now();
+  w.tprofile_batch(seeds_1_to(nseed), RG_PROFILE_TPROFILE, {tmin}, {tmax}, prof, nt, tavg);
+  const double tsec = seconds_since(t0);
+  long nsample = 0;
+  for (long k = 0; k < nseed; ++k) nsample += nt[k] != 0;
+  if (nsample == 0)
+    std::printf("%sFound no transmission eigenfunction (nsample=%ld), results will be undetermined...\n",
+                tag_warn().c_str(), nsample);
+  else
+    std::printf("%sFound %ld/%ld transmission eigenfunctions, now averaging...\n", tag_info().c_str(), nsample,
+                nseed);
+  std::vector<double> avg(nx, 0.0);
+  for (long k = 0; k < nseed; ++k)
+    if (nt[k] != 0)
+      for (int ix = 0; ix < nx; ++ix) avg[ix] = avg[ix] + prof[(size_t)k * nx + ix];
+  for (int ix = 0; ix < nx; ++ix) avg[ix] = avg[ix] / (double)nsample;
+  const std::string dir = w.generate_directory(root) + "tprofile/";
+  create_directory(dir);
+  char params[512];
+  std::snprintf(params, sizeof params,
+                "%%%% Transmission profile parameters: Found nsample=%ld / nseed=%ld, nx=%d, tmin=%s, tmax=%s, "
+                "time=%s s.\n",
+                nsample, nseed, nx, format_g0(tmin, 6).c_str(), format_g0(tmax, 6).c_str(), f0(tsec, 3).c_str());
+  const std::string raw = unique_filename(dir + "result_", ".raw.csv");
+  std::FILE* fp = open_output(raw);
+  write_header(fp, w);
+  std::fputs(params, fp);
+  std::fprintf(fp, "%%%% Here follows, on each line, the function |psi_T(x)|^2 for a given realization of the "
+                   "disorder.\n");
+  write_matrix(fp, nseed, nx, [&](size_t k, size_t ix) { return prof[k * nx + ix]; });
+  std::fclose(fp);
+  std::printf("%sRaw profile data written in file: %s\n", tag_info().c_str(), raw.c_str());
+  const std::string avgf = unique_filename(dir + "result_", ".avg.csv");
+  const std::vector<double> x = w.get_xmesh();
+  fp = open_output(avgf);
+  write_header(fp, w);
+  std::fputs(params, fp);
+  std::fprintf(fp, "x, tprofile\n");
+  for (int ix = 0; ix < nx; ++ix) std::fprintf(fp, "%s, %s\n", format_g0(x[ix]).c_str(), format_g0(avg[ix]).c_str());
+  std::fclose(fp);
+  std::printf("%sAverage profile written in file: %s\n", tag_info().c_str(), avgf.c_str());
+}
+
+// task_tprofile_group and save_tprofile_group (src/main.f90:572-728).
+void task_tprofile_group(const std::string& text, const std::string& root) {
+  constexpr int nprofile = 4;
+  const recurgreen::Parameters p = waveguide_parameters(text);
+  const NmlGroup tg = read_namelist(text, "tprofile_group", {"tm", "dt", "nseed", "nthreads"});
+  const std::vector<double> tm = nml_reals(tg, "tm", nprofile, std::vector<double>(nprofile, 0.0));
+  const std::vector<double> dt = nml_reals(tg, "dt", nprofile, std::vector<double>(nprofile, 0.0));
+  const long nseed = nml_int(tg, "nseed", 0);
+  recurgreen::Waveguide w(p);
+  w.print_parameters(stdout, strip(tag_info()));
+  if (nseed <= 0)
+    throw Stop("Invalid number of disorder realizations (received " + fmt_int(nseed) + "), aborting...");
+  const int nx = w.get_nx();
+  std::vector<double> prof, tavgdata;
+  std::vector<int32_t> nt;
+  const auto t0 = std::chrono::steady_clock::now();
+  w.tprofile_batch(seeds_1_to(nseed), RG_PROFILE_GROUP, tm, dt, prof, nt, tavgdata);
+  const double tsec = seconds_since(t0);
+  std::vector<double> avg((size_t)nx * nprofile, 0.0);
+  long nsample[nprofile] = {0, 0, 0, 0};
+  for (int ip = 0; ip < nprofile; ++ip) {
+    for (long k = 0; k < nseed; ++k) {
+      if (nt[(size_t)k * nprofile + ip] == 0) continue;
+      for (int ix = 0; ix < nx; ++ix)
+        avg[(size_t)ip * nx + ix] = avg[(size_t)ip * nx + ix] + prof[((size_t)k * nprofile + ip) * nx + ix];
+      ++nsample[ip];
+    }
+    if (nsample[ip] != 0) {
+      std::printf("%sProfile %d/%d : Found %ld/%ld transmission eigenfunctions, now averaging...\n",
+                  tag_info().c_str(), ip + 1, nprofile, nsample[ip], nseed);
+      for (int ix = 0; ix < nx; ++ix) avg[(size_t)ip * nx + ix] = avg[(size_t)ip * nx + ix] / (double)nsample[ip];
+    } else {
+      std::printf("%sProfile %d/%d : Found no transmission eigenstate (nsample=%ld), results will be "
+                  "undetermined...\n", tag_warn().c_str(), ip + 1, nprofile, nsample[ip]);
+    }
+  }
+  double tsum = 0.0;
+  for (double v : tavgdata) tsum += v;
+  const double tavg = tsum / nseed;
+  double var = 0.0;
+  for (double v : tavgdata) var += (v - tavg) * (v - tavg);
+  const double uctavg = std::sqrt(var) / nseed;
+  const std::string dir = w.generate_directory(root) + "tprofile_group/";
+  create_directory(dir);
+  const std::string fname = unique_filename(dir + "result_", ".csv");
+  const std::vector<double> x = w.get_xmesh();
+  std::FILE* fp = open_output(fname);
+  write_header(fp, w);
+  auto join6 = [](const std::vector<double>& v) {
+    std::string s;
+    for (size_t i = 0; i < v.size(); ++i) s += (i ? ", " : "") + format_g0(v[i], 6);
+    return s;
+  };
+  std::fprintf(fp, "%%%% Transmission profile parameters: nx=%d, tm=[%s], dt=[%s].\n", nx, join6(tm).c_str(),
+               join6(dt).c_str());
+  std::fprintf(fp, "%%%% Results: Found nsample=[%ld, %ld, %ld, %ld] over nseed=%ld, tavg=%s+-%s, time=%s s.\n",
+               nsample[0], nsample[1], nsample[2], nsample[3], nseed, format_g0(tavg, 6).c_str(),
+               format_g0(uctavg, 6).c_str(), f0(tsec, 3).c_str());
+  std::fprintf(fp, "x");
+  for (int ip = 0; ip < nprofile; ++ip) std::fprintf(fp, ", tprofile%s", f0(tm[ip], 4).c_str());
+  std::fprintf(fp, "\n");
+  write_matrix(fp, nx, nprofile + 1,
+               [&](size_t ix, size_t j) { return j == 0 ? x[ix] : avg[(j - 1) * nx + ix]; });
+  std::fclose(fp);
+  std::printf("%sAverage profiles written in file: %s\n", tag_info().c_str(), fname.c_str());
+}
+
+// task_tpattern (src/main.f90:735-877): the mean over seeds of |t_{b,imu}|^2
+// and |r_{b,imu}|^2 ('incident'), of their column sums ('total'), or of
+// |d_{b,imu}|^2 for the deposition matrix d at the middle of the medium from
+// the first slice ('deposition', rprob zero).
 void task_tpattern(const std::string& text, const std::string& root) {
   const NmlGroup tp = read_namelist(text, "tpattern", {"nseed", "imode", "nthreads", "probatype"});
   const long nseed = nml_int(tp, "nseed", 0);
@@ -502,54 +697,57 @@ void task_tpattern(const std::string& text, const std::string& root) {
     throw Stop("Invalid number of disorder realizations (received " + fmt_int(nseed) + "), aborting...");
   if (probatype != "incident" && probatype != "total" && probatype != "deposition")
     throw Stop("Invalid probatype, received '" + probatype + "', expected incident/total/deposition, aborting...");
-  if (probatype == "deposition")
-    throw Stop("probatype 'deposition' needs the full Green function, which this GPU build does not compute, "
-               "aborting...");
   recurgreen::Waveguide w(waveguide_parameters(text));
   const int M = w.get_nmu();
-  const long imu = w.get_parameters().boundtype == "periodic" ? (imode + M / 2 - 1) % M + 1 : imode;
+  const recurgreen::Parameters wp = w.get_parameters();
+  const long imu = wp.boundtype == "periodic" ? (imode + M / 2 - 1) % M + 1 : imode;
   if (imu < 1 || imu > M)
     throw Stop("Invalid incident mode imode=" + fmt_int(imode) + ", expected in [1, " + fmt_int(M) + "], aborting...");
+  const int fpos = wp.nxfree + wp.nxdiso / 2 + 1;  // src/main.f90:769-770
   std::vector<double> tsum(M, 0.0), rsum(M, 0.0);
   const auto t0 = std::chrono::steady_clock::now();
   const long chunk = 256;
   std::vector<std::complex<double>> t, r;
+  auto prob = [](std::complex<double> z) {  // abs(z)**2, as the reference writes it
+    const double a = std::abs(z);
+    return a * a;
+  };
   for (long s0 = 1; s0 <= nseed; s0 += chunk) {
     std::vector<int32_t> seeds;
     for (long sd = s0; sd < s0 + chunk && sd <= nseed; ++sd) seeds.push_back((int32_t)sd);
-    w.refl_trans_v1_batch(seeds, &r, t);
     const size_t mm = (size_t)M * M;
+    if (probatype == "deposition") {
+      w.deposition_batch(seeds, fpos, 1, (int)imu, t);
+      for (size_t k = 0; k < seeds.size(); ++k)
+        for (int b = 0; b < M; ++b) tsum[b] += prob(t[k * M + b]);
+      continue;
+    }
+    w.refl_trans_v1_batch(seeds, &r, t);
     for (size_t k = 0; k < seeds.size(); ++k) {  // seed order, as the Fortran sum over dim=2
       const std::complex<double>* tk = t.data() + k * mm;
       const std::complex<double>* rk = r.data() + k * mm;
-      auto prob = [](std::complex<double> z) {  // abs(z)**2, as the reference writes it
-        const double a = std::abs(z);
-        return a * a;
-      };
       for (int b = 0; b < M; ++b) {
-        double tp = 0.0, rp = 0.0;
+        double tpb = 0.0, rpb = 0.0;
         if (probatype == "incident") {
-          tp = prob(tk[(size_t)(imu - 1) * M + b]);
-          rp = prob(rk[(size_t)(imu - 1) * M + b]);
+          tpb = prob(tk[(size_t)(imu - 1) * M + b]);
+          rpb = prob(rk[(size_t)(imu - 1) * M + b]);
         } else {  // column b summed over its rows
           for (int i = 0; i < M; ++i) {
-            tp += prob(tk[(size_t)b * M + i]);
-            rp += prob(rk[(size_t)b * M + i]);
+            tpb += prob(tk[(size_t)b * M + i]);
+            rpb += prob(rk[(size_t)b * M + i]);
           }
         }
-        tsum[b] += tp;
-        rsum[b] += rp;
+        tsum[b] += tpb;
+        rsum[b] += rpb;
       }
     }
   }
-  const double tsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  const double tsec = seconds_since(t0);
   const std::string dir = w.generate_directory(root) + "tpattern/";
   create_directory(dir);
   const std::string fname = unique_filename(dir + "result_", ".csv");
-  std::FILE* fp = std::fopen(fname.c_str(), "w");
-  if (!fp) throw Stop("Cannot open file: " + fname);
-  std::fprintf(fp, "%%%% Computed on %s by %s\n", timestamp().c_str(), kProgram);
-  w.print_parameters(fp, "%%");
+  std::FILE* fp = open_output(fname);
+  write_header(fp, w);
   std::fprintf(fp, "%%%% Radiation pattern parameters: probatype='%s', nseed=%ld, imode=%ld, time=%s s.\n",
                probatype.c_str(), nseed, imode, f0(tsec, 3).c_str());
   std::fprintf(fp, "imu, tprob, rprob\n");
@@ -565,11 +763,14 @@ void execute_file(const std::string& text, const std::string& root) {
   const std::string task = nml_string(s, "task", "");
   if (task == "tdistrib") {
     task_tdistrib(text, root);
+  } else if (task == "wavefunction") {
+    task_wavefunction(text, root);
+  } else if (task == "tprofile") {
+    task_tprofile(text, root);
+  } else if (task == "tprofile_group") {
+    task_tprofile_group(text, root);
   } else if (task == "tpattern") {
     task_tpattern(text, root);
-  } else if (task == "wavefunction" || task == "tprofile" || task == "tprofile_group") {
-    throw Stop("Task '" + task + "' is not part of this GPU build, which runs the tdistrib and tpattern tasks, "
-               "aborting...");
   } else {
     throw Stop("Unknown task '" + task + "', aborting...");
   }

@@ -1,6 +1,7 @@
 // Host side of the `recurgreen` and `plothisto` programs: the settings
-// files, the tdistrib task and the re-binning of saved samples, as the
-// reference's drivers do them (src/main.f90:7-328, src/plot_histogram.f90),
+// files, the tasks (tdistrib, wavefunction, tprofile, tprofile_group,
+// tpattern) and the re-binning of saved samples, as the reference's drivers
+// do them (src/main.f90:7-877, src/plot_histogram.f90),
 // on top of the C++ interface of include/recurgreen.hpp.
 #pragma once
 
@@ -41,6 +42,8 @@ std::string nml_string(const NmlGroup& g, const std::string& key, const std::str
 long nml_int(const NmlGroup& g, const std::string& key, long def);
 double nml_real(const NmlGroup& g, const std::string& key, double def);
 bool nml_logical(const NmlGroup& g, const std::string& key, bool def);
+// An array entry (`tm = 0.1, 0.4, ...`): exactly n reals, or `def` when absent.
+std::vector<double> nml_reals(const NmlGroup& g, const std::string& key, size_t n, const std::vector<double>& def);
 
 // Fortran G0.d output as gfortran writes it (F form with d significant
 // digits for 0.1 <= |x| < 10^d, else 0.ddddE+-e).

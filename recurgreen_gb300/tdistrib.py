@@ -9,7 +9,7 @@ preamble, a `tm, rho` header, values written like Fortran's G0.16).  The
 eigenvalues come from one batched GPU launch (rg_tdistrib_batch) and the
 histogram counts from the GPU (rg_histogram).
 
-    python -m recurgreen_gb300.tdistrib settings.nml [--outdir DIR]     (task tdistrib or tpattern)
+    python -m recurgreen_gb300.tdistrib settings.nml [--outdir DIR]     (any task of &settings)
     python -m recurgreen_gb300.tdistrib --replot plothisto_settings.nml result_1.eigvals.csv
 """
 from __future__ import annotations
@@ -309,17 +309,24 @@ def _waveguide_from(wg: dict) -> Waveguide:
 
 def tpattern_probabilities(w: Waveguide, nseed: int, imu: int, probatype: str, chunk: int = 256):
     """The seed loop of task_tpattern (src/main.f90:796-836): the mean over
-    seeds 1..nseed of |t_{b,imu}|^2 and |r_{b,imu}|^2 ('incident') or of
-    sum_b |t_{ba}|^2 and sum_b |r_{ba}|^2 ('total'), from batched t and r."""
+    seeds 1..nseed of |t_{b,imu}|^2 and |r_{b,imu}|^2 ('incident'), of
+    sum_b |t_{ba}|^2 and sum_b |r_{ba}|^2 ('total'), or of |d_{b,imu}|^2 for
+    the deposition matrix d at the middle of the medium from the first slice
+    ('deposition', rprob zero), from batched GPU calls."""
     M = w.nmu
     tsum, rsum = np.zeros(M), np.zeros(M)
+    fpos = w.nxfree + w.nxdiso // 2 + 1  # src/main.f90:769-770
     for s0 in range(1, nseed + 1, chunk):
         seeds = np.arange(s0, min(s0 + chunk, nseed + 1), dtype=np.int32)
-        r, t = w.refl_trans_v1_batch(seeds)
-        if probatype == "incident":
-            tp, rp = np.abs(t[:, :, imu - 1]) ** 2, np.abs(r[:, :, imu - 1]) ** 2
+        if probatype == "deposition":
+            d = w.deposition_batch(seeds, fpos, 1, col=imu)
+            tp, rp = np.abs(d) ** 2, np.zeros((seeds.size, M))
         else:
-            tp, rp = (np.abs(t) ** 2).sum(axis=1), (np.abs(r) ** 2).sum(axis=1)
+            r, t = w.refl_trans_v1_batch(seeds)
+            if probatype == "incident":
+                tp, rp = np.abs(t[:, :, imu - 1]) ** 2, np.abs(r[:, :, imu - 1]) ** 2
+            else:
+                tp, rp = (np.abs(t) ** 2).sum(axis=1), (np.abs(r) ** 2).sum(axis=1)
         for k in range(seeds.size):  # seed order, as the Fortran sum over dim=2
             tsum += tp[k]
             rsum += rp[k]
@@ -327,9 +334,8 @@ def tpattern_probabilities(w: Waveguide, nseed: int, imu: int, probatype: str, c
 
 
 def task_tpattern(settings: dict, outdir: str = "out") -> str:
-    """task_tpattern (src/main.f90:735-838) for probatype 'incident' and
-    'total'; 'deposition' needs the full Green function inside the medium,
-    which this GPU build does not compute.  Returns the result file."""
+    """task_tpattern (src/main.f90:735-838) and save_tpattern
+    (src/main.f90:843-877).  Returns the result file."""
     tp = settings["tpattern"]
     nseed, imode = int(tp.get("nseed", 0)), int(tp.get("imode", 1))
     probatype = str(tp.get("probatype", "incident")).strip()
@@ -337,9 +343,6 @@ def task_tpattern(settings: dict, outdir: str = "out") -> str:
         raise ValueError(f"Invalid number of disorder realizations (received {nseed}), aborting...")
     if probatype not in ("incident", "total", "deposition"):
         raise ValueError(f"Invalid probatype, received '{probatype}', expected incident/total/deposition, aborting...")
-    if probatype == "deposition":
-        raise ValueError("probatype 'deposition' needs the full Green function, which this GPU build does not "
-                         "compute, aborting...")
     w = _waveguide_from(settings["waveguide"])
     M = w.nmu
     imu = (imode + M // 2 - 1) % M + 1 if w.get_parameters()["boundtype"] == "periodic" else imode
@@ -402,9 +405,17 @@ def main(argv=None) -> None:
     nml = read_namelists(open(a.settings).read())
     if a.replot:
         print(plot_histo_from_file(nml, a.datafile))
-    elif str(nml.get("settings", {}).get("task", "tdistrib")).strip() == "tpattern":
-        print(task_tpattern(nml, a.outdir))
     else:
+        task = str(nml.get("settings", {}).get("task", "tdistrib")).strip()
+        if task == "tpattern":
+            print(task_tpattern(nml, a.outdir))
+            return
+        if task in ("wavefunction", "tprofile", "tprofile_group"):
+            from . import tprofile as P
+
+            r = getattr(P, "task_" + task)(nml, a.outdir)
+            print(r if isinstance(r, str) else r.get("path") or r["avg"])
+            return
         r = task_tdistrib(nml, a.outdir)
         print(r["distrib"], f"{r['time']:.3f} s")
 

@@ -27,6 +27,22 @@ def complex_matrix(src: str, sub: str, var: str, shape):
     return {"shape": list(shape), "order": "row-major", "re_im": vals}
 
 
+def complex_array_f(src: str, sub: str, var: str, shape):
+    """A = reshape([(re, im), ...], shape(A)) inside subroutine `sub`, no
+    order= argument: Fortran (column-major) element order."""
+    body = src[src.index("subroutine " + sub):]
+    body = body[:body.index("end subroutine")]
+    body = "\n".join(l for l in body.splitlines() if not l.lstrip().startswith("!"))
+    m = re.search(var + r"\s*=\s*reshape\(\[(.*?)\],\s*shape", body, re.S)
+    pairs = re.findall(r"\(\s*([-0-9.eE]+)_wp\s*,\s*([-0-9.eE]+)_wp\s*\)", m.group(1))
+    vals = [[float(a), float(b)] for a, b in pairs]
+    n = 1
+    for d in shape:
+        n *= d
+    assert len(vals) == n
+    return {"shape": list(shape), "order": "fortran", "re_im": vals}
+
+
 def real_vector(src: str, sub: str, var: str):
     body = src[src.index("subroutine " + sub):]
     body = body[:body.index("end subroutine")]
@@ -61,7 +77,13 @@ def main(ref: str) -> None:
             "A": complex_matrix(src, "test_singular_values", "A", (4, 3)),
             "S_expc": real_vector(src, "test_singular_values", "S_expc"),
         },
-        "diagonalize_ahca": {"T_expc": real_vector(src, "test_diagonalize_ahca", "T_expc")},
+        "diagonalize_ahca": {"A": complex_matrix(src, "test_diagonalize_ahca", "A", (4, 3)),
+                             "T_expc": real_vector(src, "test_diagonalize_ahca", "T_expc")},
+        "solve_block_tridiag": {
+            "amat": complex_array_f(src, "test_solve_block_tridiag", "amat", (3, 2, 2)),
+            "imat": complex_array_f(src, "test_solve_block_tridiag", "imat", (3, 2, 1)),
+            "bdiag": real_vector(src, "test_solve_block_tridiag", "bdiag"),
+        },
         "inverse_complex": {"A": complex_matrix(src, "test_inverse_complex", "A", (4, 4))},
         "norm2_complex": {"A": complex_matrix(src, "test_norm2_complex", "A", (4, 3)), "expected": 2.646045307275178},
         "histogram": {

@@ -41,13 +41,15 @@ def test_settings_errors_stop_like_the_reference(progs, tmp_path):
     cases = {
         "unknown.nml": ("&settings task = 'nosuch' /\n", "Unknown task 'nosuch', aborting..."),
         "wavefunction.nml": ("&settings\n task = 'wavefunction'  !! c\n/\n",
-                             "Task 'wavefunction' is not part of this GPU build"),
+                             "Invalid entry in namelist: group &waveguide not found"),
         "tp_nseed.nml": ("&settings task='tpattern' /\n&tpattern nseed=0, imode=1, probatype='incident' /\n",
                          "Invalid number of disorder realizations (received 0), aborting..."),
         "tp_type.nml": ("&settings task='tpattern' /\n&tpattern nseed=4, imode=1, probatype='side' /\n",
                         "Invalid probatype, received 'side', expected incident/total/deposition, aborting..."),
-        "tp_dep.nml": ("&settings task='tpattern' /\n&tpattern nseed=4, imode=1, probatype='deposition' /\n",
-                       "probatype 'deposition' needs the full Green function"),
+        "tg_tm.nml": ("&settings task='tprofile_group' /\n&waveguide wol=5.25 /\n"
+                      "&tprofile_group\n tm = 0.1, 0.5\n nseed = 3\n/\n", "Invalid entry in namelist: tm = 0.1, 0.5"),
+        "tp_key.nml": ("&settings task='tprofile' /\n&waveguide wol=5.25 /\n&tprofile tmin=0.1, tmid=0.5 /\n",
+                       "Invalid entry in namelist:"),
         "entry.nml": ("&settings task='tdistrib' /\n&waveguide\n wol = 5.25, bogus = 3\n/\n&tdistrib nseed=2 /\n",
                       "Invalid entry in namelist: wol = 5.25, bogus = 3..."),
         "nogroup.nml": ("&settings task='tdistrib' /\n&tdistrib nseed=2 /\n",

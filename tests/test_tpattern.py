@@ -1,7 +1,7 @@
-"""The tpattern task (src/main.f90:735-877, probatype 'incident' and
-'total') on batched t and r: the batch equals single compute_refl_trans_v1
-calls, the averaged probabilities equal the oracle's, and the C++ program
-writes the Python driver's rows."""
+"""The tpattern task (src/main.f90:735-877) on batched t and r ('incident',
+'total') and on the batched deposition matrix ('deposition'): the batch
+equals single compute_refl_trans_v1 calls, the averaged probabilities equal
+the oracle's, and the C++ program writes the Python driver's rows."""
 import os
 import subprocess
 
@@ -40,6 +40,10 @@ def _oracle_pattern(kw, nseed, imu, probatype):
     M = o.nmu
     tsum, rsum = np.zeros(M), np.zeros(M)
     for s in range(1, nseed + 1):
+        if probatype == "deposition":
+            d = o.deposition_upot(o.potential(s), o.nxfree + o.nxdiso // 2 + 1, 1)
+            tsum += np.abs(d[:, imu - 1]) ** 2
+            continue
         r, t = o.refl_trans_v1_upot(o.potential(s))
         if probatype == "incident":
             tsum += np.abs(t[:, imu - 1]) ** 2
@@ -50,7 +54,7 @@ def _oracle_pattern(kw, nseed, imu, probatype):
     return tsum / nseed, rsum / nseed
 
 
-@pytest.mark.parametrize("probatype", ["incident", "total"])
+@pytest.mark.parametrize("probatype", ["incident", "total", "deposition"])
 @pytest.mark.parametrize("name", ["dirichlet_m10", "periodic_m9"])
 def test_pattern_matches_oracle(name, probatype):
     kw = GUIDES[name]
@@ -60,6 +64,9 @@ def test_pattern_matches_oracle(name, probatype):
     tp, rp = T.tpattern_probabilities(g, 7, imu, probatype, chunk=3)
     to, ro = _oracle_pattern(kw, 7, imu, probatype)
     assert np.max(np.abs(tp - to)) <= 1e-10 * np.max(np.abs(to))
+    if probatype == "deposition":
+        assert np.all(rp == 0.0)
+        return
     assert np.max(np.abs(rp - ro)) <= 1e-10 * np.max(np.abs(ro))
     if probatype == "total" and kw.get("dabso", 0.0) == 0.0:
         np.testing.assert_allclose(tp + rp, 1.0, rtol=0, atol=1e-10)  # flux per incident propagating channel
@@ -78,17 +85,19 @@ NML = """&settings
 """
 
 
-def test_cpp_program_writes_python_rows(tmp_path):
+@pytest.mark.parametrize("probatype", ["incident", "deposition"])
+def test_cpp_program_writes_python_rows(tmp_path, probatype):
     build.build()
-    (tmp_path / "s.nml").write_text(NML)
+    nml = NML.replace("probatype = 'incident'", f"probatype = '{probatype}'")
+    (tmp_path / "s.nml").write_text(nml)
     r = subprocess.run([os.path.join(build.BIN, "recurgreen"), "s.nml"], cwd=tmp_path, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     out = tmp_path / "out" / "dscat_2." / "dabso_0." / "wol_4.3" / "periodic" / "tpattern" / "result_1.csv"
     lines = out.read_text().splitlines()
-    assert lines[4].startswith("%% Radiation pattern parameters: probatype='incident', nseed=9, imode=2, time=")
+    assert lines[4].startswith(f"%% Radiation pattern parameters: probatype='{probatype}', nseed=9, imode=2, time=")
     assert lines[5] == "imu, tprob, rprob"
-    py = T.task_tpattern(T.read_namelists(NML), str(tmp_path / "py"))
+    py = T.task_tpattern(T.read_namelists(nml), str(tmp_path / "py"))
     pl = open(py).read().splitlines()
     assert pl[1:4] == lines[1:4] and pl[5] == lines[5] and len(pl) == len(lines)
     # same rows up to the libm of |t| (the C++ and numpy hypot may differ by an ulp)
