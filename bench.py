@@ -31,7 +31,12 @@ cannot be built here.
          and both gradients w.r.t. U through the adjoint sweep (both
          cotangent chains in one reverse sweep);
   large  M=512, Nx=10^4 (or --nx, then also extrapolated to 10^4 by slice
-         count), ny=2048, --batch realizations (default 152, one wave).
+         count), ny=2048, --batch realizations (default 152, one wave);
+  tprofile  the default guide (M=64, Nx=2000, ny=256, L/l_s=10): transmission-
+         eigenstate profiles for 0.9 <= T <= 1 (compute_tprofile) of --batch
+         realizations (default 304) through rg_tprofile_batch, against
+         per-realization rg_compute_tprofile calls and the oracle's
+         solve_block_tridiag + zgesvd path on one host core.
 """
 from __future__ import annotations
 
@@ -300,6 +305,43 @@ def run_workload(args) -> None:
                     "histogram_seconds": t_hist, "bad_status": int((st != 0).sum()),
                     "dense_equivalent_tflops": fl / dt / 1e12, "total_tflop": fl / 1e12, "per_N": hist})
         out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
+    elif args.workload == "tprofile":
+        import oracle as O
+
+        kw = dict(WORKLOAD, nxdiso=args.nx)
+        w = rg.Waveguide(**kw)
+        n = args.batch if args.batch != NSEED else 304
+        seeds = np.arange(1, n + 1, dtype=np.int32)
+        w.tprofile_batch(seeds[:8], "tprofile", [0.9], [1.0])  # warm-up
+        times = []
+        for _ in range(max(args.steps, 1)):
+            dt, (prof, nt, _) = _sync_time(torch, lambda: w.tprofile_batch(seeds, "tprofile", [0.9], [1.0]))
+            times.append(dt)
+        dt = min(times)
+        M, nx = w.nmu, w.nx
+        ksel = float(nt.mean())
+        fl = flops_per_realization(M, nx) + 16.0 * M * M * ksel * nx  # forward sweep + back-substitution
+        out.update({"modes": M, "nx": nx, "ny": w.ny, "realizations": n, "window": [0.9, 1.0],
+                    "mean_eigenstates_in_window": ksel, "realizations_per_s": n / dt, "seconds": dt,
+                    "dense_equivalent_tflops": fl * n / dt / 1e12,
+                    "dump_bytes_per_realization": 2 * nx * M * M * 16})
+        out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
+        if args.per_sample > 0:
+            t0 = time.perf_counter()
+            for s in range(1, args.per_sample + 1):
+                w.compute_tprofile(s, 0.9, 1.0)
+            pdt = time.perf_counter() - t0
+            out["per_realization_per_s"] = args.per_sample / pdt
+            out["batched_over_per_realization"] = out["realizations_per_s"] / out["per_realization_per_s"]
+        o = O.Waveguide(**kw)
+        cs = 2
+        t0 = time.perf_counter()
+        for s in range(1, cs + 1):
+            o.tprofile_upot(o.potential(s), 0.9, 1.0)
+        cdt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cs / cdt, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{cs} realizations (seeds 1..{cs}): solve_block_tridiag with "
+                                         f"zgetrf/zgetri/zgemm, zgesvd('N','A'), profile loop; {cdt:.1f} s"}
     elif args.workload == "diff":
         from recurgreen_gb300.adjoint import transmission_losses, transmission_losses_and_grads
 
@@ -345,7 +387,7 @@ def main() -> None:
                     help="slices (profiling runs only; the workload is Nx=2000)")
     ap.add_argument("--per-sample", type=int, default=4,
                     help="seeds timed through the per-realization drop-in call (0: skip)")
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "n256", "uneven", "diff", "large"])
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "n256", "uneven", "diff", "large", "tprofile"])
     args = ap.parse_args()
     if args.impl == "reference":
         WORKLOAD["nxdiso"] = args.nx

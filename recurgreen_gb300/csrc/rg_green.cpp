@@ -2,7 +2,9 @@
 // rg_green.cu): the reference's argument checks and messages
 // (src/waveguide.f90:636-997), device buffers sized per call, realizations
 // chunked by device memory, and the launch sequence
-//   forward sweep keeping (S_n, Z_n) of every slice (pivoted blocked kernel)
+//   forward sweep keeping (S_n, Z_n) of every slice (symmetric kernel for
+//     Dirichlet guides of up to 64 modes, pivoted blocked kernel otherwise
+//     and for the items the symmetric one flags)
 //   -> eigenvectors of t^H t and their selection (profiles)
 //   -> back-substitution on the source vectors
 //   -> window sums (profiles) or wavefunction pixels.
@@ -103,54 +105,80 @@ int chunk_size(const GreenView& v, int n, size_t per_item) {
   return (int)c;
 }
 
-// The forward sweep of nk realizations with the state of every slice kept:
-// pivoted blocked kernel, Fisher-Lee t (sqrt(real(mu)), full nmu x nmu) to
-// d_t when given, source at slice `source` (0-based).  Planned before the
-// arena is allocated: plan_sweep reserves the workspace, launch_dump_sweep
-// fills in the pointers and launches.
+// The forward sweep of nk realizations with the state of every slice kept,
+// Fisher-Lee t (sqrt(real(mu)), full nmu x nmu) to d_t when given, source at
+// slice `source` (0-based).  Dirichlet guides of up to 64 modes run the
+// symmetric shared-memory kernel (12 M^3 per slice); the items it flags, and
+// every other guide, run the pivoted blocked kernel (16 M^3), which also
+// keeps the states.  Planned before the arena is allocated: plan_sweep
+// reserves the workspace and the flag list, launch_dump_sweep fills in the
+// pointers and launches.
 struct DumpSweep {
-  rg::SweepArgs a{};
-  int grid = 0;
-  size_t off_work = 0;
+  rg::SweepArgs sym{};    // symmetric kernel (used when use_sym)
+  rg::SweepArgs piv{};    // pivoted blocked kernel: every item, or the flagged ones
+  bool use_sym = false;
+  int grid_sym = 0, grid_piv = 0;
+  size_t off_work = 0, off_flags = 0;
 };
 
 int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds) {
-  rg::SweepArgs& a = ds->a;
-  a = rg::SweepArgs{};
+  rg::SweepArgs a{};
   a.mode = rg::kModeTmat;
   a.nreal = nk;
   a.wgs = v.d_desc;
   a.work_counter = v.d_counter;
   a.max_M = v.nmu;
   a.max_ny = v.ny;
-  a.force_large = 1;
-  a.symmetric = 0;
   a.inject_at = source;
-  int64_t stride = 0;
-  int rc = rg::sweep_plan(a, v.sm_count, &ds->grid, &stride);
-  if (rc) return rc;
-  const int slots = ds->grid / (a.cluster > 0 ? a.cluster : 1);
-  a.work_stride = stride;
-  ds->off_work = ar.add(sizeof(double2) * (size_t)stride * slots);
+  ds->use_sym = v.symmetric && v.nmu <= rg::kMaxModesSmem;
+  int64_t stride = 0, stride_sym = 0;
+  int rc;
+  ds->piv = a;
+  ds->piv.force_large = 1;
+  if ((rc = rg::sweep_large_plan(ds->piv, v.sm_count, &ds->grid_piv, &stride))) return rc;
+  size_t work = sizeof(double2) * (size_t)stride * (ds->grid_piv / (ds->piv.cluster > 0 ? ds->piv.cluster : 1));
+  ds->piv.work_stride = stride;
+  if (ds->use_sym) {
+    ds->sym = a;
+    ds->sym.symmetric = 1;
+    ds->sym.sym_tau = v.sym_tau;
+    if ((rc = rg::sweep_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym))) return rc;
+    ds->sym.work_stride = stride_sym;
+    work = std::max(work, sizeof(double2) * (size_t)stride_sym * ds->grid_sym);
+    // The re-run takes the flagged items: queue length in counter 1, its
+    // own position in counter 2.
+    ds->piv.count_ptr = v.d_counter + 1;
+    ds->piv.work_counter = v.d_counter + 2;
+    ds->off_flags = ar.add(sizeof(int32_t) * (size_t)nk);
+  }
+  ds->off_work = ar.add(work);
   return RG_OK;
 }
 
-int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, const int32_t* d_seeds, const double* d_upot,
-                      double2* d_dump, double2* d_t, int32_t* d_status) {
-  rg::SweepArgs& a = ds.a;
-  a.work = ar.at<double2>(ds.off_work);
-  a.seeds = d_seeds;
-  if (d_upot) {
-    a.upot = d_upot;
-    a.pot_rstride = (int64_t)v.nxdiso * v.ny;
-    a.pot_xstride = v.ny;
-    a.pot_ystride = 1;
+int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, int nk, const int32_t* d_seeds,
+                      const double* d_upot, double2* d_dump, double2* d_t, int32_t* d_status) {
+  for (rg::SweepArgs* a : {&ds.sym, &ds.piv}) {
+    a->nreal = nk;
+    a->work = ar.at<double2>(ds.off_work);
+    a->seeds = d_seeds;
+    if (d_upot) {
+      a->upot = d_upot;
+      a->pot_rstride = (int64_t)v.nxdiso * v.ny;
+      a->pot_xstride = v.ny;
+      a->pot_ystride = 1;
+    }
+    a->state_dump = d_dump;
+    a->tout = d_t;
+    a->status = d_status;
   }
-  a.state_dump = d_dump;
-  a.tout = d_t;
-  a.status = d_status;
   RG_CUDA(cudaMemsetAsync(v.d_counter, 0, sizeof(int) * rg::kQueueCounters, v.stream));
-  return rg::launch_sweep(a, v.stream, ds.grid);
+  int rc;
+  if (ds.use_sym) {
+    ds.sym.flag_list = ar.at<int32_t>(ds.off_flags);
+    ds.piv.item_idx = ds.sym.flag_list;
+    if ((rc = rg::launch_sweep_sym(ds.sym, v.stream, ds.grid_sym))) return rc;
+  }
+  return rg::launch_sweep_large(ds.piv, v.stream, ds.grid_piv);
 }
 
 const char* status_text(int code) {
@@ -246,8 +274,7 @@ int rg_tprofile_batch(rg_waveguide* w, const int32_t* seeds, int n, int kind, in
     const int nk = std::min(chunk, n - k0);
     int32_t* d_st = ar.at<int32_t>(o_st);
     RG_CUDA(cudaMemcpyAsync(ar.at<int32_t>(o_seed), seeds + k0, sizeof(int32_t) * nk, cudaMemcpyHostToDevice, s));
-    ds.a.nreal = nk;
-    if ((rc = launch_dump_sweep(v, ds, ar, ar.at<int32_t>(o_seed), nullptr, ar.at<double2>(o_dump),
+    if ((rc = launch_dump_sweep(v, ds, ar, nk, ar.at<int32_t>(o_seed), nullptr, ar.at<double2>(o_dump),
                                 ar.at<double2>(o_t), d_st)))
       return rc;
     rg::EigvecArgs e{};
@@ -413,8 +440,7 @@ int rg_deposition_batch(rg_waveguide* w, const int32_t* seeds, int n, int fpos, 
   for (int k0 = 0; k0 < n; k0 += chunk) {
     const int nk = std::min(chunk, n - k0);
     RG_CUDA(cudaMemcpyAsync(ar.at<int32_t>(o_seed), seeds + k0, sizeof(int32_t) * nk, cudaMemcpyHostToDevice, s));
-    ds.a.nreal = nk;
-    if ((rc = launch_dump_sweep(v, ds, ar, ar.at<int32_t>(o_seed), nullptr, ar.at<double2>(o_dump), nullptr,
+    if ((rc = launch_dump_sweep(v, ds, ar, nk, ar.at<int32_t>(o_seed), nullptr, ar.at<double2>(o_dump), nullptr,
                                 ar.at<int32_t>(o_st))))
       return rc;
     rg::BackArgs bk{};
@@ -507,7 +533,7 @@ int rg_compute_wavefunction(rg_waveguide* w, int iseed, int ipos, int imode, dou
   pa.jumppoly = v.desc.jumppoly;
   pa.upot = ar.at<double>(o_pot);
   if ((rc = rg::launch_potential(pa, s))) return rc;
-  if ((rc = launch_dump_sweep(v, ds, ar, nullptr, pa.upot, ar.at<double2>(o_dump), nullptr, ar.at<int32_t>(o_st))))
+  if ((rc = launch_dump_sweep(v, ds, ar, 1, nullptr, pa.upot, ar.at<double2>(o_dump), nullptr, ar.at<int32_t>(o_st))))
     return rc;
   rg::BackArgs bk{};
   bk.nreal = 1;

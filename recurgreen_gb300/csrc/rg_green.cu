@@ -181,25 +181,27 @@ __global__ void __launch_bounds__(kNT) eigvec_kernel(EigvecArgs a) {
   if (tid == 0) a.status[r] = ok ? RG_OK : RG_ERR_NOCONV;
 }
 
-// Back-substitution.  Block (chunk, item): source vectors s0 .. s0+kKC-1 of
-// item blockIdx.y.  Each thread owns the outputs e = tid + kNT*j, row
-// m = e / kKC, vector v = e % kKC (v is the same for all j of a thread).
-// Ysh holds B Y_{n+1} and Wsh the source vectors, both [M][kKC].
+// Back-substitution.  Block (chunk, item): the nv <= kKC source vectors
+// s0 .. s0+nv-1 of item blockIdx.y.  The M*nv outputs are dealt to the
+// threads, e = tid + kNT*j -> row m = e / nv, vector v = e % nv, so the FP64
+// work is 16 M^2 nv per slice whatever nv is (an FP64 warp instruction costs
+// the same with idle lanes; whole idle warps cost nothing).  Ysh holds
+// B Y_{n+1} and Wsh the source vectors, [M][kKC]; Psh the |Y|^2 terms of
+// the profile, summed per vector in a fixed order.
 template <int JMAX>
 __global__ void __launch_bounds__(kNT) back_kernel(BackArgs a) {
   extern __shared__ double2 shb[];
   const int M = a.M;
   double2* Ysh = shb;
   double2* Wsh = shb + M * kKC;
-  __shared__ double red[kNT / 32][kKC];
+  double* Psh = (double*)(Wsh + M * kKC);
   const int r = blockIdx.y;
   const int kr = a.kcount ? a.kcount[r] : a.kmax;
   const int s0 = blockIdx.x * kKC;
   if (s0 >= kr) return;  // uniform over the block
   const int nv = min(kKC, kr - s0);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int v = tid % kKC;
-  const int J = (M * kKC + kNT - 1) / kNT;  // <= JMAX (checked by the launcher)
+  const int nout = M * nv;  // <= kNT * JMAX (checked by the launcher)
   for (int e = tid; e < M * kKC; e += kNT) {
     const int m = e / kKC, vv = e % kKC;
     Wsh[e] = vv < nv ? a.src[(int64_t)r * a.src_stride + (int64_t)(s0 + vv) * M + m] : make_double2(0.0, 0.0);
@@ -208,6 +210,13 @@ __global__ void __launch_bounds__(kNT) back_kernel(BackArgs a) {
   __syncthreads();
   const int64_t mm = (int64_t)M * M;
   const int nslices = a.only_lo ? 1 : a.nx - a.i_lo;
+  int mj[JMAX], vj[JMAX];  // row and vector of output j (the divisions once, outside the slice loop)
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) {
+    const int e = tid + kNT * j;
+    mj[j] = e < nout ? e / nv : 0;
+    vj[j] = e < nout ? e % nv : 0;
+  }
   for (int n = a.nx - 1; n >= a.i_lo; --n) {
     const double2* S = a.dump + ((int64_t)r * a.nx + n) * 2 * mm;
     const double2* Z = S + mm;
@@ -215,17 +224,17 @@ __global__ void __launch_bounds__(kNT) back_kernel(BackArgs a) {
     double2 acc[JMAX];
 #pragma unroll
     for (int j = 0; j < JMAX; ++j) acc[j] = make_double2(0.0, 0.0);
-    for (int c = 0; c < M; ++c) {
-      const double2 wc = Wsh[c * kKC + v];
-      const double2 yc = Ysh[c * kKC + v];
+    if (tid < nout) {
+      for (int c = 0; c < M; ++c) {
 #pragma unroll
-      for (int j = 0; j < JMAX; ++j) {
-        if (j < J) {
-          const int m = (tid + kNT * j) / kKC;
-          if (m < M) {
+        for (int j = 0; j < JMAX; ++j) {
+          if (tid + kNT * j < nout) {
+            const int m = mj[j], v = vj[j];
+            const double2 wc = Wsh[c * kKC + v];
             const double2 z = __ldg(Z + (int64_t)m * M + c);
             acc[j] = make_double2(fma(z.x, wc.x, fma(-z.y, wc.y, acc[j].x)), fma(z.x, wc.y, fma(z.y, wc.x, acc[j].y)));
             if (!first) {
+              const double2 yc = Ysh[c * kKC + v];
               const double2 sv = __ldg(S + (int64_t)m * M + c);
               acc[j] = make_double2(fma(-sv.x, yc.x, fma(sv.y, yc.y, acc[j].x)),
                                     fma(-sv.x, yc.y, fma(-sv.y, yc.x, acc[j].y)));
@@ -235,39 +244,33 @@ __global__ void __launch_bounds__(kNT) back_kernel(BackArgs a) {
       }
     }
     __syncthreads();  // every thread has read Ysh
-    double p = 0.0;
 #pragma unroll
     for (int j = 0; j < JMAX; ++j) {
-      if (j < J) {
-        const int m = (tid + kNT * j) / kKC;
-        if (m < M) {
-          const double2 y = acc[j];
-          Ysh[m * kKC + v] = cmul(a.bmat[m], y);
-          p = fma(y.x, y.x, fma(y.y, y.y, p));
-          if (a.out_mode == kBackColumns && v < nv && (!a.only_lo || n == a.i_lo)) {
-            const int64_t sl = a.only_lo ? 0 : n - a.i_lo;
-            double2 o = y;
-            if (a.left) {
-              const double2 q = cmul(a.left[m], y);
-              o = make_double2(-2.0 * q.y, 2.0 * q.x);
-            }
-            a.cols[(((int64_t)r * nslices + sl) * a.kmax + s0 + v) * M + m] = o;
+      if (tid + kNT * j < nout) {
+        const int m = mj[j], v = vj[j];
+        const double2 y = acc[j];
+        Ysh[m * kKC + v] = cmul(a.bmat[m], y);
+        Psh[m * kKC + v] = fma(y.x, y.x, y.y * y.y);
+        if (a.out_mode == kBackColumns && (!a.only_lo || n == a.i_lo)) {
+          const int64_t sl = a.only_lo ? 0 : n - a.i_lo;
+          double2 o = y;
+          if (a.left) {
+            const double2 q = cmul(a.left[m], y);
+            o = make_double2(-2.0 * q.y, 2.0 * q.x);
           }
+          a.cols[(((int64_t)r * nslices + sl) * a.kmax + s0 + v) * M + m] = o;
         }
       }
     }
+    __syncthreads();  // Ysh and Psh complete
     if (a.out_mode == kBackProfile) {
-      // lanes v, v+8, v+16, v+24 of a warp share the vector; then the warps.
-      p += __shfl_xor_sync(0xffffffffu, p, 8);
-      p += __shfl_xor_sync(0xffffffffu, p, 16);
-      if (lane < kKC) red[warp][lane] = p;
-    }
-    __syncthreads();  // Ysh and red complete
-    if (a.out_mode == kBackProfile && tid < nv) {
-      double s = 0.0;
+      for (int v = warp; v < nv; v += kNT / 32) {  // warp v sums vector v over the rows
+        double p = 0.0;
+        for (int m = lane; m < M; m += 32) p += Psh[m * kKC + v];
 #pragma unroll
-      for (int w = 0; w < kNT / 32; ++w) s += red[w][tid];
-      a.prof[((int64_t)r * a.kmax + s0 + tid) * a.nx + n] = s;
+        for (int off = 16; off; off >>= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
+        if (lane == 0) a.prof[((int64_t)r * a.kmax + s0 + v) * a.nx + n] = p;
+      }
     }
   }
 }
@@ -315,7 +318,7 @@ __global__ void wavefun_kernel(WavefunArgs a) {
 
 template <int JMAX>
 int launch_back_t(const BackArgs& a, cudaStream_t s) {
-  const size_t smem = sizeof(double2) * 2 * (size_t)a.M * kKC;
+  const size_t smem = (2 * sizeof(double2) + sizeof(double)) * (size_t)a.M * kKC;
   RG_CUDA(cudaFuncSetAttribute(back_kernel<JMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const dim3 grid((a.kmax + kKC - 1) / kKC, a.nreal);
   back_kernel<JMAX><<<grid, kNT, smem, s>>>(a);
@@ -343,7 +346,7 @@ int launch_back(const BackArgs& a, cudaStream_t s) {
   if (a.nreal <= 0 || a.kmax <= 0) return RG_OK;
   if (a.i_lo < 0 || a.i_lo >= a.nx) return fail(RG_ERR_INVALID_ARG, "back-substitution: slice out of range");
   const int J = (a.M * kKC + kNT - 1) / kNT;
-  if (2 * (size_t)a.M * kKC * sizeof(double2) > 200 * 1024)
+  if ((2 * sizeof(double2) + sizeof(double)) * (size_t)a.M * kKC > 200 * 1024)
     return fail(RG_ERR_INVALID_ARG, "back-substitution: too many modes");
   if (J <= 2) return launch_back_t<2>(a, s);
   if (J <= 4) return launch_back_t<4>(a, s);

@@ -180,6 +180,8 @@ struct GreenView {
   const double* ymesh;   // host [ny]
   const double* kpmesh;  // host [nmu]
   const cplx* sqmu_r;    // host [nmu] sqrt(real(mu))
+  int symmetric;         // the symmetric sweep is enabled for this guide (Dirichlet)
+  double sym_tau;        // its pivot threshold
 };
 int green_view(const rg_waveguide* w, GreenView* out);
 

@@ -482,7 +482,7 @@ int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
     // The symmetric blocked kernel, unless segment states are asked for (the
     // adjoint's recomputation forces the pivoted one); the pivoted re-run
     // uses the same cluster size, grid and workspace.
-    if (!a.symmetric || a.force_large || a.state_in || a.state_dump || a.state_out) {
+    if (!a.symmetric || a.force_large || a.state_in || a.state_dump || a.state_out || a.inject_at) {
       a.symmetric = 0;
       return sweep_large_plan(a, sm_count, grid, work_stride);
     }
@@ -502,13 +502,15 @@ int sweep_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
     *work_stride = std::max(*work_stride, s2);
     return RG_OK;
   }
+  // The shared-memory kernels run whole guides from slice 0 and keep no
+  // per-slice states (the symmetric one keeps them when launched directly).
+  if (a.n_end != 0 || a.state_in || a.state_dump || a.state_out || a.inject_at)
+    return fail(RG_ERR_INVALID_ARG, "sweep: segment arguments need the blocked kernel (force_large)");
   int rc;
   if (a.max_M <= 16) rc = plan_t<16, 64, 8>(a, sm_count, grid, work_stride);
   else if (a.max_M <= 32) rc = plan_t<32, 128, 4>(a, sm_count, grid, work_stride);
   else rc = plan_t<64, 256, 2>(a, sm_count, grid, work_stride);
   if (rc || !a.symmetric) return rc;
-  if (a.n_end != 0 || a.state_in || a.state_dump || a.state_out)
-    return fail(RG_ERR_INVALID_ARG, "symmetric sweep: segment arguments are not supported");
   int g2 = 0;
   int64_t s2 = 0;
   if ((rc = sweep_sym_plan(a, sm_count, &g2, &s2))) return rc;

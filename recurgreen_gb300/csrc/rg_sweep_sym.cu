@@ -91,11 +91,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
       s_M = M;
       s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
     }
+    // R starts as the identity source at slice 0, or as zero when the source
+    // is at a later slice (a.inject_at).
+    const double one = a.inject_at > 0 ? 0.0 : 1.0;
 #pragma unroll
     for (int ai = 0; ai < AMAX; ++ai)
 #pragma unroll
       for (int b = 0; b < CB; ++b)
-        R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? 1.0 : 0.0, 0.0);
+        R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? one : 0.0, 0.0);
     if (draw) {
       // Each generator state is set up by the thread that draws from it (the
       // pair (j, ny-1-j) of the projection step).
@@ -206,7 +209,15 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
           W[i * LDW + j] = x;
         }
       }
-      if (n > 0) {
+      if (n > 0 && n == a.inject_at) {
+        // The identity source at this slice: Z_n = S_n I, stored as R = -S_n
+        // (Gs1 = -R after slice 0), so the right-hand side is -I.
+#pragma unroll
+        for (int ai = 0; ai < AMAX; ++ai)
+#pragma unroll
+          for (int b = 0; b < CB; ++b)
+            R[ai][b] = make_double2((warp + NW * ai) == (lane + 32 * b) ? -1.0 : 0.0, 0.0);
+      } else if (n > 0) {
 #pragma unroll
         for (int ai = 0; ai < AMAX; ++ai) {
           const int q = warp + NW * ai;
@@ -343,6 +354,26 @@ __global__ void __launch_bounds__(NT, MINB) sweep_sym_kernel(SweepArgs a) {
           }
         }
         __syncthreads();
+      }
+      if (a.state_dump) {
+        // The state after this slice, natural order: Gss = W (symmetric) and
+        // Gs1 = sign * R, the solve_block_tridiag pair (S_n, Z_n).
+        double2* d1 = a.state_dump + ((int64_t)r * nx + n) * 2 * M * M;
+        for (int e = tid; e < M * M; e += NT) {
+          const int i = e / M, j = e % M;
+          d1[e] = i <= j ? W[i * LDW + j] : W[j * LDW + i];
+        }
+        const double gs = (n == 0) ? 1.0 : -1.0;
+#pragma unroll
+        for (int ai = 0; ai < AMAX; ++ai) {
+          const int q = warp + NW * ai;
+#pragma unroll
+          for (int b = 0; b < CB; ++b) {
+            const int j = lane + 32 * b;
+            if (q < M && j < M) d1[(int64_t)M * M + q * M + j] = cscale(gs, R[ai][b]);
+          }
+        }
+        __syncthreads();  // W is read before the next slice overwrites it
       }
     }
 

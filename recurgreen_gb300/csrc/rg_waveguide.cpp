@@ -817,6 +817,9 @@ int green_view(const rg_waveguide* w, GreenView* out) {
   out->ymesh = w->ymesh.data();
   out->kpmesh = w->kpmesh.data();
   out->sqmu_r = w->sqmu_r.data();
+  const SweepArgs a = make_args(w, kModeEig);
+  out->symmetric = a.symmetric;
+  out->sym_tau = a.sym_tau;
   return RG_OK;
 }
 
