@@ -162,7 +162,7 @@ int rg_compute_tprofile_group(rg_waveguide* wg, int iseed, int nprofile, const d
 int rg_compute_deposition(rg_waveguide* wg, int iseed, int fpos, int ipos, double* depmat);
 
 /* Deposition for n realizations (the deposition branch of the tpattern
- * task, src/main.f90:802-806): col in 1..nmu gives column col of each
+ * task, src/main.f90:804-809): col in 1..nmu gives column col of each
  * realization's depmat (out + 2*k*nmu), col == 0 the whole matrix
  * (out + 2*k*nmu*nmu).  Host pointers; status may be NULL. */
 int rg_deposition_batch(rg_waveguide* wg, const int32_t* seeds, int n, int fpos, int ipos, int col, double* out,
