@@ -107,16 +107,16 @@ int chunk_size(const GreenView& v, int n, size_t per_item) {
 
 // The forward sweep of nk realizations with the state of every slice kept,
 // Fisher-Lee t (sqrt(real(mu)), full nmu x nmu) to d_t when given, source at
-// slice `source` (0-based).  Dirichlet guides of up to 64 modes run the
-// symmetric shared-memory kernel (12 M^3 per slice); the items it flags, and
-// every other guide, run the pivoted blocked kernel (16 M^3), which also
-// keeps the states.  Planned before the arena is allocated: plan_sweep
+// slice `source` (0-based).  Dirichlet guides run a symmetric kernel (12 M^3
+// per slice): the shared-memory one up to 64 modes, the blocked one above;
+// the items it flags, and periodic guides, run the pivoted blocked kernel
+// (16 M^3), which also keeps the states.  Planned before the arena is allocated: plan_sweep
 // reserves the workspace and the flag list, launch_dump_sweep fills in the
 // pointers and launches.
 struct DumpSweep {
   rg::SweepArgs sym{};    // symmetric kernel (used when use_sym)
   rg::SweepArgs piv{};    // pivoted blocked kernel: every item, or the flagged ones
-  bool use_sym = false;
+  bool use_sym = false, sym_blocked = false;
   int grid_sym = 0, grid_piv = 0;
   size_t off_work = 0, off_flags = 0;
 };
@@ -130,7 +130,8 @@ int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds)
   a.max_M = v.nmu;
   a.max_ny = v.ny;
   a.inject_at = source;
-  ds->use_sym = v.symmetric && v.nmu <= rg::kMaxModesSmem;
+  ds->use_sym = v.symmetric != 0;
+  ds->sym_blocked = v.nmu > rg::kMaxModesSmem;
   int64_t stride = 0, stride_sym = 0;
   int rc;
   ds->piv = a;
@@ -142,9 +143,12 @@ int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds)
     ds->sym = a;
     ds->sym.symmetric = 1;
     ds->sym.sym_tau = v.sym_tau;
-    if ((rc = rg::sweep_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym))) return rc;
+    rc = ds->sym_blocked ? rg::sweep_large_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym)
+                         : rg::sweep_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym);
+    if (rc) return rc;
     ds->sym.work_stride = stride_sym;
-    work = std::max(work, sizeof(double2) * (size_t)stride_sym * ds->grid_sym);
+    const int slots_sym = ds->grid_sym / (ds->sym.cluster > 0 ? ds->sym.cluster : 1);
+    work = std::max(work, sizeof(double2) * (size_t)stride_sym * slots_sym);
     // The re-run takes the flagged items: queue length in counter 1, its
     // own position in counter 2.
     ds->piv.count_ptr = v.d_counter + 1;
@@ -176,7 +180,9 @@ int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, int nk
   if (ds.use_sym) {
     ds.sym.flag_list = ar.at<int32_t>(ds.off_flags);
     ds.piv.item_idx = ds.sym.flag_list;
-    if ((rc = rg::launch_sweep_sym(ds.sym, v.stream, ds.grid_sym))) return rc;
+    rc = ds.sym_blocked ? rg::launch_sweep_large_sym(ds.sym, v.stream, ds.grid_sym)
+                        : rg::launch_sweep_sym(ds.sym, v.stream, ds.grid_sym);
+    if (rc) return rc;
   }
   return rg::launch_sweep_large(ds.piv, v.stream, ds.grid_piv);
 }

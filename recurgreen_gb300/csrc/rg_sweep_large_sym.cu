@@ -30,7 +30,9 @@
 // column flags the realization (kStatusNeedPivot, appended to flag_list);
 // launch_sweep then re-runs the flagged ones with the pivoted blocked kernel.
 // Periodic items (Hermitian, not symmetric) are flagged at once.  Segment
-// mode supports a stop after n_end slices (no Fisher-Lee stage), not states.
+// mode supports a stop after n_end slices (no Fisher-Lee stage); a whole
+// sweep can keep the state of every slice (state_dump) and start its source
+// at a later slice (inject_at), not resume from a state.
 #include <cooperative_groups.h>
 
 #include "rg_device.cuh"
@@ -163,7 +165,8 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
     double* urow_g = (double*)(gen + 4 * ny);     // [ny] paired potential row
     double2* PR = (double2*)(urow_g + ((ny + 1) & ~1)) + (int64_t)rank * NB * M;  // [NB][M] this CTA's raw pivot columns
     if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
-    for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? 1.0 : 0.0, 0.0);
+    const double one = a.inject_at > 0 ? 0.0 : 1.0;  // the source at slice 0, or zero until inject_at
+    for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? one : 0.0, 0.0);
     if (draw) {
       // Each generator state is set up by the thread that draws from it (the
       // pair (j, ny-1-j) below), so it is only ever read and written from one
@@ -261,7 +264,10 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           if (n > 0) x = csub(x, cmul(cmul(wd.bmat[i], __ldcg(W + e)), wd.bmat[j]));
           W[e] = x;
         }
-        if (n > 0) Rg[e] = cmul(wd.bmat[i], cscale(rsign, __ldcg(Rg + e)));
+        // At the source slice the right-hand side is -I (Gs1 = -R after slice 0).
+        if (n > 0)
+          Rg[e] = (n == a.inject_at) ? make_double2(i == j ? -1.0 : 0.0, 0.0)
+                                     : cmul(wd.bmat[i], cscale(rsign, __ldcg(Rg + e)));
       }
       cluster.sync();
       unsigned long long best = 0ULL;
@@ -528,6 +534,19 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           }
         }
         cluster.sync();
+      }
+      if (a.state_dump && *status0 != kStatusNeedPivot) {
+        // The state after this slice, natural order: Gss = W (symmetric,
+        // upper triangle) and Gs1 = sign * R, the solve_block_tridiag pair
+        // (S_n, Z_n).
+        double2* d1 = a.state_dump + ((int64_t)r * wd.nx + n) * 2 * mm;
+        const double gs = (n == 0) ? 1.0 : -1.0;
+        for (int64_t e = ctid; e < mm; e += CNT) {
+          const int i = (int)(e / M), j = (int)(e % M);
+          d1[e] = __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i));
+          d1[mm + e] = cscale(gs, __ldcg(Rg + e));
+        }
+        cluster.sync();  // W and R are read before the next slice rewrites them
       }
     }
 

@@ -188,24 +188,26 @@ def test_gpu_tprofile_batch_is_the_single_call():
 
 
 @pytest.mark.gpu
-def test_gpu_symmetric_and_pivoted_states_agree(monkeypatch):
-    """Dirichlet guides keep their slice states from the symmetric sweep; with
-    every item flagged (RG_SYM_TAU huge) or the symmetric sweep off
-    (RG_SYMMETRIC=0) the pivoted blocked kernel keeps them instead."""
-    w, o = _pair(nxdiso=70)
+@pytest.mark.parametrize("kw", [dict(nxdiso=70), dict(nxdiso=30, nxfree=1, wol=33.3, dscat=0.5)])
+def test_gpu_symmetric_and_pivoted_states_agree(monkeypatch, kw):
+    """Dirichlet guides keep their slice states from a symmetric sweep (the
+    shared-memory kernel up to 64 modes, the blocked one above); with every
+    item flagged (RG_SYM_TAU huge) or the symmetric sweep off (RG_SYMMETRIC=0)
+    the pivoted blocked kernel keeps them instead."""
+    w, o = _pair(**kw)
     seeds = np.arange(1, 7, dtype=np.int32)
     base, nt0, _ = w.tprofile_batch(seeds, "tprofile", [0.2], [0.99])
-    dep = w.deposition_batch(seeds, 40, 11)
+    dep = w.deposition_batch(seeds, 20, 11)
     for var, val in (("RG_SYM_TAU", "1e300"), ("RG_SYMMETRIC", "0")):
         monkeypatch.setenv(var, val)
         p, nt, _ = w.tprofile_batch(seeds, "tprofile", [0.2], [0.99])
         np.testing.assert_array_equal(nt, nt0)
         assert _rel(p, base) < 1e-10
-        d = w.deposition_batch(seeds, 40, 11)
+        d = w.deposition_batch(seeds, 20, 11)
         assert np.linalg.norm(d - dep) / np.linalg.norm(dep) < 1e-10
         monkeypatch.delenv(var)
     u = w.potential(3)
-    do = o.deposition_upot(u, 40, 11)
+    do = o.deposition_upot(u, 20, 11)
     assert np.linalg.norm(dep[2] - do) / np.linalg.norm(do) < 1e-10
 
 
