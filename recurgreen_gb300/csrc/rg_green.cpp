@@ -14,6 +14,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -21,6 +22,8 @@
 #include "rg_internal.h"
 
 using rg::cplx;
+using rg::DeviceGuard;
+using rg::status_text;
 using rg::GreenView;
 
 namespace {
@@ -47,18 +50,6 @@ std::string g0(double x, int d) {
   }
   return sign + "0." + digits + "E" + (e10 < 0 ? "-" : "+") + std::to_string(std::abs(e10));
 }
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
 
 // One device allocation carved into 256-byte aligned pieces.
 class Arena {
@@ -91,7 +82,10 @@ class Arena {
 
 // Realizations per launch: what fits in half the free device memory (at most
 // 96 GiB), rounded down to whole waves of two CTAs per SM when larger.
+// RG_GREEN_CHUNK=k caps it at k (tests use it to run several chunks).
 int chunk_size(const GreenView& v, int n, size_t per_item) {
+  const char* cap = std::getenv("RG_GREEN_CHUNK");
+  const long cap_n = (cap && *cap) ? std::strtol(cap, nullptr, 10) : 0;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
     cudaGetLastError();
@@ -102,6 +96,7 @@ int chunk_size(const GreenView& v, int n, size_t per_item) {
   c = std::max<int64_t>(1, std::min<int64_t>(c, n));
   const int wave = 2 * v.sm_count;
   if (c > wave && c < n) c -= c % wave;
+  if (cap_n > 0 && c > cap_n) c = cap_n;
   return (int)c;
 }
 
@@ -185,14 +180,6 @@ int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, int nk
     if (rc) return rc;
   }
   return rg::launch_sweep_large(ds.piv, v.stream, ds.grid_piv);
-}
-
-const char* status_text(int code) {
-  switch (code) {
-    case RG_ERR_SINGULAR: return "zgetrf: Matrix is numerically singular (zero or NaN pivot)";
-    case RG_ERR_NOCONV: return "singular values did not converge";
-    default: return "error";
-  }
 }
 
 int check_window_args(const GreenView& v, int kind, int nprof, const double* a, const double* b) {

@@ -26,6 +26,28 @@ int cuda_fail(cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return ::rg::cuda_fail(e_, #call); \
   } while (0)
 
+// Switches to a handle's device for the duration of a call.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Message of a per-realization status.
+inline const char* status_text(int code) {
+  switch (code) {
+    case RG_ERR_SINGULAR: return "zgetrf: Matrix is numerically singular (zero or NaN pivot)";
+    case RG_ERR_NOCONV: return "singular values did not converge";
+    default: return "error";
+  }
+}
+
 // Largest mode count the shared-memory sweep kernel handles.
 constexpr int kMaxModesSmem = 64;
 

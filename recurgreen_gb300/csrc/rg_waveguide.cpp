@@ -16,6 +16,8 @@
 #include "rg_internal.h"
 
 using rg::cplx;
+using rg::DeviceGuard;
+using rg::status_text;
 
 namespace rg {
 
@@ -209,19 +211,6 @@ struct rg_waveguide {
 namespace {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
-
-// Switches to the handle's device for the duration of a call.
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
 
 template <class T>
 int upload(T** dst, const void* src, size_t bytes) {
@@ -679,14 +668,6 @@ int first_bad_status(const int32_t* st, int n) {
   for (int k = 0; k < n; ++k)
     if (st[k] != RG_OK) return st[k];
   return RG_OK;
-}
-
-const char* status_text(int code) {
-  switch (code) {
-    case RG_ERR_SINGULAR: return "zgetrf: Matrix is numerically singular (zero or NaN pivot)";
-    case RG_ERR_NOCONV: return "singular values did not converge";
-    default: return "error";
-  }
 }
 
 // Single realization with either a seed or a host potential.  mode selects

@@ -212,6 +212,23 @@ def test_gpu_symmetric_and_pivoted_states_agree(monkeypatch, kw):
 
 
 @pytest.mark.gpu
+def test_gpu_chunked_batches_equal_one_launch(monkeypatch):
+    """Realizations run in chunks bounded by device memory; chunks of 3 give
+    the bits of one launch, for the profiles and the deposition."""
+    w, _ = _pair("periodic", nxdiso=50, wol=3.6)
+    seeds = np.array([5, 1, 9, 2, 7, 3, 8], np.int32)
+    p0, nt0, ta0 = w.tprofile_batch(seeds, "group", [0.2, 0.7], [0.2, 0.3])
+    d0 = w.deposition_batch(seeds, 30, 4, col=2)
+    monkeypatch.setenv("RG_GREEN_CHUNK", "3")
+    p1, nt1, ta1 = w.tprofile_batch(seeds, "group", [0.2, 0.7], [0.2, 0.3])
+    d1 = w.deposition_batch(seeds, 30, 4, col=2)
+    np.testing.assert_array_equal(p1, p0)
+    np.testing.assert_array_equal(nt1, nt0)
+    np.testing.assert_array_equal(ta1, ta0)
+    np.testing.assert_array_equal(d1, d0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("bt,kw", [("dirichlet", {}), ("periodic", dict(wol=3.6))])
 def test_gpu_deposition_matches_oracle(bt, kw):
     w, o = _pair(bt, **kw)
