@@ -365,6 +365,8 @@ def run_workload(args) -> None:
         t_fwd, _ = _sync_time(torch, fwd)
         t_all, (g1, g2) = _sync_time(torch, step)
         fl = flops_per_realization(w.nmu, w.nx)
+        from recurgreen_gb300.adjoint import _method
+        out.update({"adjoint_method": _method(w, U, "auto")})
         out.update({"modes": w.nmu, "nx": w.nx, "ny": w.ny, "realizations": n, "checkpoint_every": K,
                     "forward_seconds": t_fwd, "forward_and_two_gradients_seconds": t_all,
                     "realizations_per_s_with_gradients": n / t_all,

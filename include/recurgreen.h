@@ -241,6 +241,18 @@ int rg_sweep_segment(rg_waveguide* wg, const double* d_upot, int n, int n_begin,
 int rg_adjoint_grad_rows(rg_waveguide* wg, const double* d_xbar, int n, double* d_grad, int64_t grad_stride,
                          void* stream);
 
+/* A whole sweep on caller-given potentials d_upot (n x nxdiso x ny, C order)
+ * that keeps the state of every slice: d_states (n x nx x 2 x nmu x nmu
+ * complex, row-major; NULL: none kept) receives (Gss, Gs1) after each slice, i.e. the
+ * (S_n, Z_n) of solve_block_tridiag (src/base_utils.f90:318-324) for the
+ * identity source at slice 1; d_tfilt (n x ncol x nrow complex, optional) the
+ * filtered Fisher-Lee t, d_teig (n x neigv) the eigenvalues, d_status (n) the
+ * statuses.  Dirichlet guides run the symmetric sweep.  Device pointers,
+ * enqueued on `stream` (taken literally), which is synchronised before
+ * returning.  The full-Green-function adjoint's forward pass. */
+int rg_sweep_states(rg_waveguide* wg, const double* d_upot, int n, double* d_states, double* d_tfilt,
+                    double* d_teig, int32_t* d_status, void* stream);
+
 /* Tracing (the reference times its seed loop with date_and_time,
  * src/main.f90:145,174-176): device time in milliseconds of the sweep
  * launches of the last rg_tdistrib_batch[_device] call on this handle (one

@@ -5,23 +5,40 @@ L1 = Tr(t^H t) and L2 = Tr((t^H t)^2) of the filtered Fisher-Lee matrix t
 (src/waveguide.f90:443-445) for potentials U of shape (B, nxdiso, ny)
 (float64, CUDA; U[r, ix, iy] is upot(ix, iy) of realization r), and its
 backward gives dL/dU for every grid cell.  The reference has no gradients;
-this is new functionality behind the same sweep.
+this is new functionality behind the same sweep.  Dirichlet guides only.
 
-Forward: the sweep runs in segments of K ~ sqrt(Nx) slices on the GPU
-(rg_sweep_segment), keeping only the state (Gss, Gs1) at segment ends.
+Two backward methods give the same gradient:
 
-Backward: reverse-mode through the recursion, with Gamma = dL/dt*:
+"green" (default when a realization's slice states fit in memory).  With
+H the block tridiagonal system matrix and G = H^-1, t = 2i S G(N,1) S on
+the filter window (S = diag sqrt(mu)), and dH_nn = -dV_n:
+  dL = 2 Re Tr(Gamma^H dt),  dt = -2i S G(N,n) dH_nn G(n,1) S
+so the slice-matrix adjoint is Xbar_n^H = K_n = -2i G(n,1) P G(N,n) with
+P = S Gamma~^H S (Gamma~ = Gamma embedded in M x M).  A Dirichlet H is
+complex symmetric, so G(N,n) = G(n,N)^T, and both columns of G come from one
+forward sweep that keeps every slice's (S_n, Z_n) (rg_sweep_states, the
+forward loop of solve_block_tridiag, src/base_utils.f90:318-324):
+  G(n,1) = Z_n - S_n B G(n+1,1),   G(N,1) = Z_N,
+  G(n,N) = -S_n B G(n+1,N),        G(N,N) = S_N
+(its backward loop, :327-330, once with the source at slice 1 and once at
+slice N).  Per slice: 8 M^3 for each column and 16 M^3 per loss, against
+the recursion's reverse mode below, which also recomputes the forward.
+
+"checkpoint" (O(sqrt(Nx)) states).  Forward in segments of K ~ sqrt(Nx)
+slices (rg_sweep_segment), keeping only the states at segment ends; reverse
+mode through the recursion, with Gamma = dL/dt*:
   Gs1bar_N = -2i conj(S) Gamma conj(S)          (t = 2i S Gs1_N S)
   for n = N-1 .. 0 (states recomputed segment by segment from checkpoints):
     Gssbar_n += -Gs1bar_n (B Gs1_{n-1})^H        (Gs1_n = -Gss_n B Gs1_{n-1})
     Gs1bar_{n-1} = -conj(B) Gss_n^H Gs1bar_n
     Xbar_n = -Gss_n^H Gssbar_n Gss_n^H           (Gss_n = inv(X_n))
-    dL/dU_n = -2 sum Re(Xbar_n[a][c]) chi_a chi_c (rg_adjoint_grad_rows)
     Gssbar_{n-1} = -conj(B) Xbar_n conj(B)       (X_n = A_n - V_n - B Gss_{n-1} B)
   (slice 0: Gs1_0 = Gss_0, so Gssbar_0 += Gs1bar_0).
-The per-slice complex products are batched over realizations (cuBLAS through
-torch); the recomputation and the gradient rows are this library's kernels.
-Dirichlet guides only.
+
+In both, dL/dU_n = -2 sum Re(Xbar_n[a][c]) chi_a chi_c (rg_adjoint_grad_rows).
+The per-slice complex products are batched over realizations and losses
+(cuBLAS through torch); the sweeps and the gradient rows are this library's
+kernels.
 """
 from __future__ import annotations
 
@@ -75,10 +92,17 @@ class TransmissionLosses(torch.autograd.Function):
     """(L1, L2) = (Tr t^H t, Tr (t^H t)^2) per realization, with the adjoint backward."""
 
     @staticmethod
-    def forward(ctx, U: torch.Tensor, wg: Waveguide, K: int = 0):
-        L1, L2, U, t, ckpt, K = _forward(U, wg, K)
+    def forward(ctx, U: torch.Tensor, wg: Waveguide, K: int = 0, method: str = "auto"):
+        method = _method(wg, U, method)
+        if method == "green":
+            U = _check_input(U, wg)
+            t = _green_t(wg, U)
+            ckpt = torch.empty(0, device=U.device)
+            L1, L2 = _losses(t)
+        else:
+            L1, L2, U, t, ckpt, K = _forward(U, wg, K)
         ctx.save_for_backward(U, t, ckpt)
-        ctx.wg, ctx.K = wg, K
+        ctx.wg, ctx.K, ctx.method = wg, K, method
         return L1, L2
 
     @staticmethod
@@ -88,17 +112,117 @@ class TransmissionLosses(torch.autograd.Function):
         g1 = torch.zeros(B, dtype=torch.float64, device=dev) if g1 is None else g1
         g2 = torch.zeros(B, dtype=torch.float64, device=dev) if g2 is None else g2
         Gamma = g1[:, None, None] * t + g2[:, None, None] * 2.0 * (t @ (t.conj().transpose(1, 2) @ t))
-        dU = _reverse_sweep(ctx.wg, U, ckpt, ctx.K, Gamma[None])
-        return dU[0], None, None
+        if ctx.method == "green":
+            dU = _green_backward(ctx.wg, U, lambda b0, b1, tc: Gamma[None, b0:b1])
+        else:
+            dU = _reverse_sweep(ctx.wg, U, ckpt, ctx.K, Gamma[None])
+        return dU[0], None, None, None
 
 
-def _forward(U: torch.Tensor, wg: Waveguide, K: int):
-    """Checkpointed forward sweep: (L1, L2, t, checkpoints, K)."""
+def _check_input(U: torch.Tensor, wg: Waveguide) -> torch.Tensor:
     if wg.get_parameters()["boundtype"] != "dirichlet":
         raise RecurGreenError(1, "the adjoint supports Dirichlet guides only")
     U = U.detach().contiguous()
     if U.dtype != torch.float64 or U.dim() != 3 or U.shape[1:] != (wg.nxdiso, wg.ny) or not U.is_cuda:
         raise RecurGreenError(1, f"U must be a CUDA float64 tensor of shape (B, {wg.nxdiso}, {wg.ny})")
+    return U
+
+
+def _losses(t: torch.Tensor):
+    A = t.conj().transpose(1, 2) @ t
+    return (t.abs() ** 2).sum((1, 2)), (A.abs() ** 2).sum((1, 2))
+
+
+def _states_bytes(wg: Waveguide) -> int:
+    return 2 * wg.nx * wg.nmu * wg.nmu * 16
+
+
+def _method(wg: Waveguide, U: torch.Tensor, method: str) -> str:
+    """"green" when one realization's states take at most a quarter of the
+    free device memory (then realizations run in chunks that fit), else
+    "checkpoint"."""
+    if method in ("green", "checkpoint"):
+        return method
+    if method != "auto":
+        raise RecurGreenError(1, f"unknown adjoint method '{method}'")
+    free, _ = torch.cuda.mem_get_info(U.device)
+    return "green" if _states_bytes(wg) <= free // 4 else "checkpoint"
+
+
+def _chunk(wg: Waveguide, U: torch.Tensor) -> int:
+    """Realizations whose states fit in half the free device memory (one
+    launch for the differentiation workload, which fills the GPU best)."""
+    free, _ = torch.cuda.mem_get_info(U.device)
+    return max(1, min(U.shape[0], int((free // 2) // _states_bytes(wg))))
+
+
+def _states(wg: Waveguide, U: torch.Tensor, keep: bool = True):
+    """One forward sweep of the realizations of U, keeping every slice's
+    state when asked: (states (n, nx, 2, M, M) or None, t (n, nrow, ncol))."""
+    n, M, dev = U.shape[0], wg.nmu, U.device
+    nrow, ncol = wg.imax - wg.imin + 1, wg.jmax - wg.jmin + 1
+    states = torch.empty(n, wg.nx, 2, M, M, dtype=torch.complex128, device=dev) if keep else None
+    tf = torch.empty(n, ncol, nrow, dtype=torch.complex128, device=dev)
+    teig = torch.empty(n, wg.neigv, dtype=torch.float64, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    _check(lib().rg_sweep_states(wg._h, _ptr(U), n, _ptr(states), _ptr(tf), _ptr(teig), _ptr(st),
+                                 _vp(torch.cuda.current_stream().cuda_stream)))
+    bad = st.cpu().numpy()
+    if np.any(bad != 0):
+        raise RecurGreenError(int(bad[bad != 0][0]), "singular slice matrix in the adjoint sweep")
+    return states, tf.transpose(1, 2)
+
+
+def _green_t(wg: Waveguide, U: torch.Tensor) -> torch.Tensor:
+    """The filtered t of every realization: one sweep, no states kept."""
+    _, t = _states(wg, U, keep=False)
+    return t.contiguous()
+
+
+def _green_backward(wg: Waveguide, U: torch.Tensor, gamma_of):
+    """dL/dU (S, B, nxdiso, ny) by the full-Green-function method.  For each
+    chunk [b0, b1) of realizations, gamma_of(b0, b1, t_chunk) gives the
+    cotangents Gamma (S, b1-b0, nrow, ncol) of the S losses."""
+    M, nx, dev = wg.nmu, wg.nx, U.device
+    mu, bm = wg.get_modes()
+    sq = torch.from_numpy(np.sqrt(mu)).to(dev)
+    bvec = torch.from_numpy(bm).to(dev)[:, None]
+    r0, c0 = wg.imin - 1, wg.jmin - 1
+    nxdiso, ny, nxfree = wg.nxdiso, wg.ny, wg.nxfree
+    stream = _vp(torch.cuda.current_stream().cuda_stream)
+    c = _chunk(wg, U)
+    out = None
+    for b0 in range(0, U.shape[0], c):
+        b1 = min(b0 + c, U.shape[0])
+        states, t = _states(wg, U[b0:b1])
+        Gamma = gamma_of(b0, b1, t)
+        S = Gamma.shape[0]
+        if out is None:
+            out = torch.zeros((S,) + tuple(U.shape), dtype=U.dtype, device=dev)
+        G = torch.zeros(S, b1 - b0, M, M, dtype=torch.complex128, device=dev)
+        G[:, :, r0:r0 + Gamma.shape[2], c0:c0 + Gamma.shape[3]] = Gamma
+        P = sq[:, None] * G.conj().transpose(-1, -2) * sq[None, :]  # S Gamma~^H S
+        dU = torch.zeros(S, b1 - b0, nxdiso, ny, dtype=U.dtype, device=dev)
+        X1 = states[:, nx - 1, 1].clone()  # G(N,1) = Z_N
+        XN = states[:, nx - 1, 0].clone()  # G(N,N) = S_N
+        for n in reversed(range(nx)):
+            if n < nx - 1:
+                Sn = states[:, n, 0]
+                X1 = states[:, n, 1] - Sn @ (bvec * X1)
+                XN = -(Sn @ (bvec * XN))
+            idd = n - nxfree
+            if 0 <= idd < nxdiso:
+                K = ((-2j) * ((X1 @ P) @ XN.transpose(-1, -2))).contiguous()
+                _check(lib().rg_adjoint_grad_rows(wg._h, _ptr(K), S * (b1 - b0), _vp(dU.data_ptr() + 8 * idd * ny),
+                                                  nxdiso * ny, stream))
+        out[:, b0:b1] = dU
+        del states
+    return out
+
+
+def _forward(U: torch.Tensor, wg: Waveguide, K: int):
+    """Checkpointed forward sweep: (L1, L2, t, checkpoints, K)."""
+    U = _check_input(U, wg)
     K = K or max(1, int(math.ceil(math.sqrt(wg.nx))))
     sw = _Sweeper(wg, U, K)
     M, B = sw.M, sw.B
@@ -113,9 +237,7 @@ def _forward(U: torch.Tensor, wg: Waveguide, K: int):
         else:
             t = tf.transpose(1, 2).contiguous()  # (B, nrow, ncol)
     sw.check_status()
-    A = t.conj().transpose(1, 2) @ t
-    L1 = (t.abs() ** 2).sum((1, 2))
-    L2 = (A.abs() ** 2).sum((1, 2))
+    L1, L2 = _losses(t)
     return L1, L2, U, t, ckpt, K
 
 
@@ -165,16 +287,30 @@ def _reverse_sweep(wg: Waveguide, U: torch.Tensor, ckpt: torch.Tensor, K: int, G
     return dU
 
 
-def transmission_losses(U: torch.Tensor, wg: Waveguide, K: int = 0):
-    """(Tr t^H t, Tr (t^H t)^2) per realization, differentiable in U."""
-    return TransmissionLosses.apply(U, wg, K)
+def transmission_losses(U: torch.Tensor, wg: Waveguide, K: int = 0, method: str = "auto"):
+    """(Tr t^H t, Tr (t^H t)^2) per realization, differentiable in U.
+    method: "green", "checkpoint" or "auto" (green when the states fit)."""
+    return TransmissionLosses.apply(U, wg, K, method)
 
 
-def transmission_losses_and_grads(U: torch.Tensor, wg: Waveguide, K: int = 0):
-    """(L1, L2, dL1/dU, dL2/dU) with both gradients from one reverse sweep:
-    the two cotangent chains (dL1/dt* = t, dL2/dt* = 2 t t^H t) share the
-    recomputed forward states and run as one batch.  Same values as two
-    torch.autograd.grad calls through transmission_losses."""
+def transmission_losses_and_grads(U: torch.Tensor, wg: Waveguide, K: int = 0, method: str = "auto"):
+    """(L1, L2, dL1/dU, dL2/dU) with both gradients from one backward pass:
+    the two cotangents (dL1/dt* = t, dL2/dt* = 2 t t^H t) share the states
+    and run as one batch.  With the green method the forward sweep that
+    keeps the states also gives t, so a realization is swept once.  Same
+    values as two torch.autograd.grad calls through transmission_losses."""
+    method = _method(wg, U, method)
+    if method == "green":
+        U = _check_input(U, wg)
+        ts = {}
+
+        def gamma_of(b0, b1, t):
+            ts[b0] = t
+            return torch.stack([t, 2.0 * (t @ (t.conj().transpose(1, 2) @ t))])
+
+        dU = _green_backward(wg, U, gamma_of)
+        L1, L2 = _losses(torch.cat([ts[k] for k in sorted(ts)]))
+        return L1, L2, dU[0], dU[1]
     L1, L2, Ud, t, ckpt, K = _forward(U, wg, K)
     Gamma = torch.stack([t, 2.0 * (t @ (t.conj().transpose(1, 2) @ t))])
     dU = _reverse_sweep(wg, Ud, ckpt, K, Gamma)

@@ -116,9 +116,9 @@ struct DumpSweep {
   size_t off_work = 0, off_flags = 0;
 };
 
-int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds) {
+int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds, int mode = rg::kModeTmat) {
   rg::SweepArgs a{};
-  a.mode = rg::kModeTmat;
+  a.mode = mode;
   a.nreal = nk;
   a.wgs = v.d_desc;
   a.work_counter = v.d_counter;
@@ -155,7 +155,9 @@ int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds)
 }
 
 int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, int nk, const int32_t* d_seeds,
-                      const double* d_upot, double2* d_dump, double2* d_t, int32_t* d_status) {
+                      const double* d_upot, double2* d_dump, double2* d_t, int32_t* d_status,
+                      double* d_teig = nullptr, cudaStream_t stream = nullptr) {
+  cudaStream_t st = stream ? stream : v.stream;
   for (rg::SweepArgs* a : {&ds.sym, &ds.piv}) {
     a->nreal = nk;
     a->work = ar.at<double2>(ds.off_work);
@@ -168,18 +170,19 @@ int launch_dump_sweep(const GreenView& v, DumpSweep& ds, const Arena& ar, int nk
     }
     a->state_dump = d_dump;
     a->tout = d_t;
+    a->teig = d_teig;
     a->status = d_status;
   }
-  RG_CUDA(cudaMemsetAsync(v.d_counter, 0, sizeof(int) * rg::kQueueCounters, v.stream));
+  RG_CUDA(cudaMemsetAsync(v.d_counter, 0, sizeof(int) * rg::kQueueCounters, st));
   int rc;
   if (ds.use_sym) {
     ds.sym.flag_list = ar.at<int32_t>(ds.off_flags);
     ds.piv.item_idx = ds.sym.flag_list;
-    rc = ds.sym_blocked ? rg::launch_sweep_large_sym(ds.sym, v.stream, ds.grid_sym)
-                        : rg::launch_sweep_sym(ds.sym, v.stream, ds.grid_sym);
+    rc = ds.sym_blocked ? rg::launch_sweep_large_sym(ds.sym, st, ds.grid_sym)
+                        : rg::launch_sweep_sym(ds.sym, st, ds.grid_sym);
     if (rc) return rc;
   }
-  return rg::launch_sweep_large(ds.piv, v.stream, ds.grid_piv);
+  return rg::launch_sweep_large(ds.piv, st, ds.grid_piv);
 }
 
 int check_window_args(const GreenView& v, int kind, int nprof, const double* a, const double* b) {
@@ -558,6 +561,28 @@ int rg_compute_wavefunction(rg_waveguide* w, int iseed, int ipos, int imode, dou
   RG_CUDA(cudaMemcpyAsync(&st, ar.at<int32_t>(o_st), sizeof st, cudaMemcpyDeviceToHost, s));
   RG_CUDA(cudaStreamSynchronize(s));
   if (st != RG_OK) return rg::fail(st, status_text(st));
+  return RG_OK;
+}
+
+int rg_sweep_states(rg_waveguide* w, const double* d_upot, int n, double* d_states, double* d_tfilt, double* d_teig,
+                    int32_t* d_status, void* stream) {
+  GreenView v{};
+  int rc = rg::green_view(w, &v);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!d_upot || !d_teig || !d_status)))
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_states: invalid argument");
+  if (n == 0) return RG_OK;
+  DeviceGuard g(v.device);
+  cudaStream_t s = (cudaStream_t)stream;  // taken literally: 0 is CUDA's default stream
+  Arena ar;
+  DumpSweep ds;
+  if ((rc = plan_sweep(v, n, 0, ar, &ds, rg::kModeEig))) return rc;
+  if ((rc = ar.alloc())) return rc;
+  rc = launch_dump_sweep(v, ds, ar, n, nullptr, d_upot, (double2*)d_states, (double2*)d_tfilt, d_status, d_teig,
+                         s ? s : cudaStreamLegacy);
+  if (rc) return rc;
+  // The workspace is freed when this call returns: wait for the sweep.
+  RG_CUDA(cudaStreamSynchronize(s ? s : cudaStreamLegacy));
   return RG_OK;
 }
 
