@@ -6,8 +6,10 @@ files in the same layout (`%%` preamble, header line, values written like
 Fortran's G0.16).  The per-realization work (the block tridiagonal solve,
 the eigenvectors of t^H t and the profiles) runs in the GPU library
 (rg_tprofile_batch, rg_compute_wavefunction); the seed loop is one batched
-call instead of an OpenMP loop.  The TikZ plots the reference renders after
-saving (tikz/*.py through execute_command_line) are not part of this build.
+call instead of an OpenMP loop, or, with a process group, one batched call
+per GPU on its seed range (replicas: no exchange until the gather).  The
+TikZ plots the reference renders after saving (tikz/*.py through
+execute_command_line) are not part of this build.
 """
 from __future__ import annotations
 
@@ -18,6 +20,42 @@ import numpy as np
 
 from .tdistrib import (_preamble, _waveguide_from, fortran_f, fortran_g0, generate_directory,
                        unique_filename)
+
+
+def _profiles(w, nseed: int, kind: str, a, b, group=None):
+    """Profiles of seeds 1..nseed: (prof (nseed, nprofile, nx), nt (nseed,
+    nprofile), tavg (nseed,), seconds).  With a process group (one process per
+    GPU) each rank sweeps a contiguous seed range and the results are
+    gathered in seed order on every rank; the time is the slowest rank's."""
+    a, b = np.atleast_1d(a), np.atleast_1d(b)
+    if group is None:
+        t0 = time.perf_counter()
+        prof, nt, tavg = w.tprofile_batch(np.arange(1, nseed + 1, dtype=np.int32), kind, a, b)
+        return prof, nt, tavg, time.perf_counter() - t0
+    import torch.distributed as dist
+
+    from . import replicas
+
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    seeds = replicas.seed_range(rank, world, nseed)
+    t0 = time.perf_counter()
+    if seeds.size:
+        prof, nt, tavg = w.tprofile_batch(seeds, kind, a, b)
+    else:
+        prof, nt, tavg = np.zeros((0, a.size, w.nx)), np.zeros((0, a.size), np.int32), np.zeros(0)
+    tsec = replicas.max_over_ranks(time.perf_counter() - t0, group)
+    prof = replicas.gather_values(prof.reshape(-1), group).reshape(nseed, a.size, w.nx)
+    nt = replicas.gather_values(nt.reshape(-1).astype(np.float64), group).reshape(nseed, a.size).astype(np.int32)
+    tavg = replicas.gather_values(tavg, group)
+    return prof, nt, tavg, tsec
+
+
+def _writer(group) -> bool:
+    if group is None:
+        return True
+    import torch.distributed as dist
+
+    return dist.get_rank(group) == 0
 
 
 def _header(w, prefix: str = "%%") -> list[str]:
@@ -50,27 +88,29 @@ def task_wavefunction(settings: dict, outdir: str = "out") -> str:
     return path
 
 
-def task_tprofile(settings: dict, outdir: str = "out") -> dict:
+def task_tprofile(settings: dict, outdir: str = "out", group=None) -> dict:
     """task_tprofile and save_tprofile (src/main.f90:405-565): the profile of
     every realization (raw file) and their average over the realizations
-    with at least one eigenvalue in [tmin, tmax] (avg file)."""
+    with at least one eigenvalue in [tmin, tmax] (avg file).  With a process
+    group the seeds are sharded over the ranks and rank 0 writes the files."""
     tp = settings["tprofile"]
     tmin, tmax = float(tp.get("tmin", 0.0)), float(tp.get("tmax", 1.0))
     nseed = int(tp.get("nseed", 0))
     w = _waveguide_from(settings["waveguide"])
     if nseed <= 0:
         raise ValueError(f"Invalid number of disorder realizations (received {nseed}), aborting...")
-    t0 = time.perf_counter()
-    prof, nt, _ = w.tprofile_batch(np.arange(1, nseed + 1, dtype=np.int32), "tprofile", [tmin], [tmax])
-    tsec = time.perf_counter() - t0
+    prof, nt, _, tsec = _profiles(w, nseed, "tprofile", tmin, tmax, group)
     data = prof[:, 0, :]
     nsample = int(np.count_nonzero(nt[:, 0]))
     avg = np.zeros(w.nx)
-    for k in range(nseed):  # seed order, as src/main.f90:477-482
+    for k in range(nseed):  # seed order, as src/main.f90:476-483
         if nt[k, 0] != 0:
             avg = avg + data[k]
     with np.errstate(invalid="ignore", divide="ignore"):
         avg = avg / nsample
+    res = {"raw": None, "avg": None, "nsample": nsample, "time": tsec, "profiles": data, "nt": nt[:, 0]}
+    if not _writer(group):
+        return res
     ddir = os.path.join(generate_directory(w, outdir), "tprofile")
     os.makedirs(ddir, exist_ok=True)
     params = (f"%% Transmission profile parameters: Found nsample={nsample} / nseed={nseed}, nx={w.nx}, "
@@ -91,13 +131,15 @@ def task_tprofile(settings: dict, outdir: str = "out") -> dict:
         f.write("x, tprofile\n")
         for ix in range(w.nx):
             f.write(f"{fortran_g0(float(x[ix]))}, {fortran_g0(float(avg[ix]))}\n")
-    return {"raw": raw, "avg": avgp, "nsample": nsample, "time": tsec, "profiles": data, "nt": nt[:, 0]}
+    res.update(raw=raw, avg=avgp)
+    return res
 
 
-def task_tprofile_group(settings: dict, outdir: str = "out") -> dict:
+def task_tprofile_group(settings: dict, outdir: str = "out", group=None) -> dict:
     """task_tprofile_group and save_tprofile_group (src/main.f90:572-728):
     four profiles per realization, their averages, and the mean transmission
-    Tavg with its uncertainty."""
+    Tavg with its uncertainty.  With a process group the seeds are sharded
+    over the ranks and rank 0 writes the file."""
     tg = settings["tprofile_group"]
     tm = np.atleast_1d(np.asarray(tg.get("tm", []), np.float64))
     dt = np.atleast_1d(np.asarray(tg.get("dt", []), np.float64))
@@ -108,12 +150,10 @@ def task_tprofile_group(settings: dict, outdir: str = "out") -> dict:
     w = _waveguide_from(settings["waveguide"])
     if nseed <= 0:
         raise ValueError(f"Invalid number of disorder realizations (received {nseed}), aborting...")
-    t0 = time.perf_counter()
-    prof, nt, tavgdata = w.tprofile_batch(np.arange(1, nseed + 1, dtype=np.int32), "group", tm, dt)
-    tsec = time.perf_counter() - t0
+    prof, nt, tavgdata, tsec = _profiles(w, nseed, "group", tm, dt, group)
     avg = np.zeros((w.nx, nprofile))
     nsample = np.zeros(nprofile, np.int64)
-    for ip in range(nprofile):  # src/main.f90:657-675
+    for ip in range(nprofile):  # src/main.f90:633-651
         for k in range(nseed):
             if nt[k, ip] != 0:
                 avg[:, ip] = avg[:, ip] + prof[k, ip]
@@ -122,6 +162,9 @@ def task_tprofile_group(settings: dict, outdir: str = "out") -> dict:
             avg[:, ip] = avg[:, ip] / nsample[ip]
     tavg = np.sum(tavgdata) / nseed
     uctavg = np.sqrt(np.sum((tavgdata - tavg) ** 2)) / nseed
+    res = {"path": None, "nsample": nsample, "tavg": tavg, "uctavg": uctavg, "time": tsec}
+    if not _writer(group):
+        return res
     ddir = os.path.join(generate_directory(w, outdir), "tprofile_group")
     os.makedirs(ddir, exist_ok=True)
     path = unique_filename(os.path.join(ddir, "result_"), ".csv")
@@ -137,4 +180,5 @@ def task_tprofile_group(settings: dict, outdir: str = "out") -> dict:
         f.write("x" + "".join(f", tprofile{fortran_f(float(v), 4)}" for v in tm) + "\n")
         for ix in range(w.nx):
             f.write(", ".join(fortran_g0(float(v)) for v in [x[ix], *avg[ix]]) + "\n")
-    return {"path": path, "nsample": nsample, "tavg": tavg, "uctavg": uctavg, "time": tsec}
+    res["path"] = path
+    return res

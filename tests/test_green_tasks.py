@@ -145,3 +145,30 @@ def test_cpp_program_writes_python_rows(tmp_path, task):
                 assert la.split("time=")[0].split("tavg=")[0] == lb.split("time=")[0].split("tavg=")[0]
             else:
                 assert la == lb
+
+
+@pytest.mark.parametrize("task", ["tprofile", "tprofile_group"])
+def test_tprofile_tasks_replica_path_matches(tmp_path, task):
+    """The sharded path (a process group; here one gloo rank) writes the
+    single-process rows."""
+    import torch.distributed as dist
+
+    group_nml = {"tprofile": f"&tprofile\n tmin = {TMIN}, tmax = {TMAX}, nseed = 5\n/\n",
+                 "tprofile_group": f"&tprofile_group\n tm = {', '.join(map(str, TM))}, dt = {', '.join(map(str, DT))}\n"
+                                   " nseed = 4\n/\n"}[task]
+    nml = T.read_namelists(_nml(task, group_nml))
+    one = getattr(P, "task_" + task)(nml, str(tmp_path / "one"))
+    dist.init_process_group("gloo", store=dist.HashStore(), rank=0, world_size=1)
+    try:
+        rep = getattr(P, "task_" + task)(nml, str(tmp_path / "rep"), group=dist.group.WORLD)
+    finally:
+        dist.destroy_process_group()
+    files = [("raw", "avg")] if task == "tprofile" else [("path",)]
+    for key in files[0]:
+        a, b = open(one[key]).read().splitlines(), open(rep[key]).read().splitlines()
+        assert a[1:4] == b[1:4] and len(a) == len(b)
+        for la, lb in zip(a[4:], b[4:]):
+            if la.startswith("%%"):
+                assert la.split("time=")[0] == lb.split("time=")[0]
+            else:
+                assert la == lb
