@@ -282,6 +282,18 @@ inline std::vector<double> histogram(const std::vector<double>& samples, const s
   return h;
 }
 
+// diagonalize_ahca (src/base_utils.f90:394-444) on the GPU: T (n values,
+// descending) and U (n x n, column-major) with A^H A = U diag(T) U^H for the
+// m x n column-major matrix a.
+inline void diagonalize_ahca(const std::vector<std::complex<double>>& a, int m, int n, std::vector<double>& T,
+                             std::vector<std::complex<double>>& U) {
+  if ((int64_t)a.size() != (int64_t)m * n) throw Error(RG_ERR_INVALID_ARG, "diagonalize_ahca: a is not m x n");
+  T.resize(n);
+  U.resize((size_t)n * n);
+  check(rg_diagonalize_ahca(reinterpret_cast<const double*>(a.data()), m, n, T.data(),
+                            reinterpret_cast<double*>(U.data())));
+}
+
 }  // namespace recurgreen
 
 #endif  // RECURGREEN_HPP
