@@ -3,7 +3,8 @@
  *
  * A drop-in for the `waveguide` module of RecurGreen (src/waveguide.f90): the
  * same ten waveguide parameters, one transmission computation per disorder
- * realization, and the transmission-eigenvalue distribution task.  Every entry
+ * realization, the transmission-eigenvalue distribution task, and the
+ * full-Green-function methods (profiles, deposition, wavefunction).  Every entry
  * point takes plain pointers and sizes; all arithmetic is IEEE double /
  * double complex (complex values are interleaved (re, im) pairs, matrices are
  * column-major with leading dimension = number of rows, as in Fortran).
