@@ -169,6 +169,14 @@ int rg_compute_deposition(rg_waveguide* wg, int iseed, int fpos, int ipos, doubl
 int rg_deposition_batch(rg_waveguide* wg, const int32_t* seeds, int n, int fpos, int ipos, int col, double* out,
                         int32_t* status);
 
+/* compute_refl_trans_v2 (src/waveguide.f90:526-553): t and r (r may be NULL)
+ * from the full block tridiagonal solve with the identity source at slice 1,
+ * t = 2i sqrt(real(mu)) G(x_nx; x_1) sqrt(real(mu)) and
+ * r = -1 + 2i sqrt(real(mu)) G(x_1; x_1) sqrt(real(mu)); nmu x nmu complex,
+ * column-major (host).  The reference's cross-check of v1 (its
+ * test_green_v1_v2, src/waveguide.f90:598-623). */
+int rg_compute_refl_trans_v2(rg_waveguide* wg, int iseed, double* rmat, double* tmat);
+
 /* compute_wavefunction (src/waveguide.f90:636-698): the field of a unit
  * source in mode imode at slice ipos, as the (nx*ny) x 5 table [x, y, Re psi,
  * Im psi, upot] (host, column-major; rows = nx*ny). */

@@ -5,7 +5,7 @@
  * (src/waveguide.f90:13-73): the constructor is `init`, the copy constructor
  * `init_copy`, the destructor `del`, and the type-bound procedures keep their
  * names (get_nmu, get_neigv, get_nx, get_xmesh, get_parameters,
- * compute_tdistrib, compute_refl_trans_v1, compute_wavefunction,
+ * compute_tdistrib, compute_refl_trans_v1, compute_refl_trans_v2, compute_wavefunction,
  * compute_deposition, compute_itx_profile, compute_tprofile,
  * compute_tprofile_group, print_parameters, generate_directory).  Where the reference prints a message and stops
  * (src/base_utils.f90:56-57), these methods throw recurgreen::Error carrying
@@ -230,6 +230,15 @@ class Waveguide {
     out.resize(seeds.size() * (size_t)get_nmu() * (col > 0 ? 1 : get_nmu()));
     check(rg_deposition_batch(h_, seeds.data(), (int)seeds.size(), fpos, ipos, col,
                               reinterpret_cast<double*>(out.data()), nullptr));
+  }
+  // compute_refl_trans_v2 (src/waveguide.f90:526-553): nmu x nmu, column-major.
+  void compute_refl_trans_v2(int iseed, std::vector<std::complex<double>>& rmat,
+                             std::vector<std::complex<double>>& tmat) {
+    const size_t n = (size_t)get_nmu() * get_nmu();
+    rmat.resize(n);
+    tmat.resize(n);
+    check(rg_compute_refl_trans_v2(h_, iseed, reinterpret_cast<double*>(rmat.data()),
+                                   reinterpret_cast<double*>(tmat.data())));
   }
   // compute_wavefunction (src/waveguide.f90:636-698): (nx*ny) x 5, column-major
   // (columns x, y, Re psi, Im psi, upot).

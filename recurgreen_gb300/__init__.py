@@ -30,7 +30,7 @@ EXPORTS = (
     "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info", "rg_refl_trans_v1_batch",
     "rg_tprofile_batch", "rg_compute_tprofile", "rg_compute_itx_profile", "rg_compute_tprofile_group",
     "rg_compute_deposition", "rg_deposition_batch", "rg_compute_wavefunction", "rg_diagonalize_ahca",
-    "rg_sweep_states",
+    "rg_sweep_states", "rg_compute_refl_trans_v2",
 )
 PROFILE_KINDS = {"tprofile": 0, "itx": 1, "group": 2}
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
     L.rg_compute_wavefunction.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, i64]
     L.rg_diagonalize_ahca.argtypes = [vp, C.c_int, C.c_int, dp, vp]
     L.rg_sweep_states.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp]
+    L.rg_compute_refl_trans_v2.argtypes = [vp, C.c_int, vp, vp]
     _LIB = L
     return L
 
@@ -238,6 +239,21 @@ class Waveguide:
         r = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
         _check(lib().rg_refl_trans_v1_upot(self._h, _dp(upot), r.ctypes.data if want_r else None, t.ctypes.data))
         return (r, t) if want_r else t
+
+    def compute_refl_trans_v2(self, iseed: int):
+        """compute_refl_trans_v2 (src/waveguide.f90:526-553): (r, t) from the
+        full block tridiagonal solve."""
+        t = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        r = np.zeros((self.nmu, self.nmu), np.complex128, order="F")
+        _check(lib().rg_compute_refl_trans_v2(self._h, int(iseed), r.ctypes.data, t.ctypes.data))
+        return r, t
+
+    def test_green_v1_v2(self, iseed: int):
+        """test_green_v1_v2 (src/waveguide.f90:598-623): (||r_v1 - r_v2||,
+        ||t_v1 - t_v2||), both expected 0."""
+        r1, t1 = self.compute_refl_trans_v1(iseed)
+        r2, t2 = self.compute_refl_trans_v2(iseed)
+        return float(np.linalg.norm(r1 - r2)), float(np.linalg.norm(t1 - t2))
 
     def test_unitarity(self, iseed: int) -> float:
         """test_unitarity (src/waveguide.f90:561-590): ||t^H t + r^H r - 1||."""

@@ -473,6 +473,21 @@ int rg_compute_deposition(rg_waveguide* w, int iseed, int fpos, int ipos, double
   return rg_deposition_batch(w, &s, 1, fpos, ipos, 0, depmat, nullptr);
 }
 
+int rg_compute_refl_trans_v2(rg_waveguide* w, int iseed, double* rmat, double* tmat) {
+  GreenView v{};
+  int rc = rg::green_view(w, &v);
+  if (rc) return rc;
+  if (!tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v2: NULL argument");
+  // src/waveguide.f90:526-553: the full solve with the identity source at
+  // slice 1; t = 2i sqmu X_nx sqmu, r = -1 + 2i sqmu X_1 sqmu.
+  if ((rc = rg_compute_deposition(w, iseed, v.nx, 1, tmat))) return rc;
+  if (rmat) {
+    if ((rc = rg_compute_deposition(w, iseed, 1, 1, rmat))) return rc;
+    for (int i = 0; i < v.nmu; ++i) rmat[2 * ((size_t)i * v.nmu + i)] -= 1.0;
+  }
+  return RG_OK;
+}
+
 int rg_compute_wavefunction(rg_waveguide* w, int iseed, int ipos, int imode, double* wfundata, int64_t rows) {
   GreenView v{};
   int rc = rg::green_view(w, &v);

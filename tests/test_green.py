@@ -307,3 +307,17 @@ def test_gpu_full_green_argument_checks():
         assert msg in str(e.value), (msg, str(e.value))
         assert e.value.code == rg.RG_ERR_INVALID_ARG
     assert math.isfinite(w.compute_tprofile(1, 0.0, 1.0)[0].sum())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bt,kw", [("dirichlet", dict(dabso=0.3)), ("periodic", dict(wol=3.6))])
+def test_gpu_refl_trans_v2_and_green_v1_v2(bt, kw):
+    """compute_refl_trans_v2 (the full solve) equals the oracle's v2 and the GPU's
+    v1; test_green_v1_v2 reports norms near zero, as the reference expects."""
+    w, o = _pair(bt, **kw)
+    r2, t2 = w.compute_refl_trans_v2(5)
+    ro, to = o.refl_trans_v2_upot(w.potential(5))
+    assert np.linalg.norm(t2 - to) / np.linalg.norm(to) < 1e-10
+    assert np.linalg.norm(r2 - ro) / np.linalg.norm(ro) < 1e-10
+    nr, nt = w.test_green_v1_v2(5)
+    assert nr < 1e-10 * np.linalg.norm(ro) and nt < 1e-10 * np.linalg.norm(to)
