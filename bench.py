@@ -410,9 +410,9 @@ def main() -> None:
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)  # before the NCCL group, which binds to the current device
     if world > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.init()
 
     w = rg.Waveguide(**WORKLOAD)
