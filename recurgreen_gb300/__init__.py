@@ -255,9 +255,12 @@ class Waveguide:
         r2, t2 = self.compute_refl_trans_v2(iseed)
         return float(np.linalg.norm(r1 - r2)), float(np.linalg.norm(t1 - t2))
 
-    def test_unitarity(self, iseed: int) -> float:
-        """test_unitarity (src/waveguide.f90:561-590): ||t^H t + r^H r - 1||."""
-        r, t = self.compute_refl_trans_v1(iseed)
+    def test_unitarity(self, iseed: int, version: int = 1) -> float:
+        """test_unitarity (src/waveguide.f90:561-590): ||t^H t + r^H r - 1||
+        for the v1 recursion (version 1) or the full solve (version 2)."""
+        if version not in (1, 2):
+            raise RecurGreenError(RG_ERR_INVALID_ARG, "Unknown recursive Green version (must be 1 or 2), aborting...")
+        r, t = self.compute_refl_trans_v1(iseed) if version == 1 else self.compute_refl_trans_v2(iseed)
         d = t.conj().T @ t + r.conj().T @ r - np.eye(self.nmu)
         return float(np.sqrt(np.sum((d * d.conj()).real)))
 

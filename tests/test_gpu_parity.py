@@ -101,6 +101,10 @@ def test_unitarity_on_gpu(seed):
     conserved at dabso = 0, ||t^H t + r^H r - 1|| ~ 0, through the seed-driven C ABI call."""
     g = rg.Waveguide(**CASES["ref_test"])
     assert g.test_unitarity(seed) < 1e-10
+    assert g.test_unitarity(seed, version=2) < 1e-10
+    # test_green_v1_v2 (src/waveguide.f90:598-623) on src/waveguide.test.f90:95-122's guide
+    nr, nt = g.test_green_v1_v2(seed)
+    assert nr < 1e-10 and nt < 1e-10
     o = O.Waveguide(**CASES["ref_test"])
     ro, to = o.refl_trans_v1_upot(o.potential(seed))
     r, t = g.compute_refl_trans_v1(seed)
