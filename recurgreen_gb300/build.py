@@ -23,7 +23,8 @@ LIB = os.path.join(PKG, "librecurgreen_gb300.so")
 HOST = os.path.join(PKG, "host")
 BIN = os.path.join(PKG, "bin")
 HOST_SOURCES = ["driver.cpp"]
-PROGRAMS = {"recurgreen": "recurgreen_main.cpp", "plothisto": "plothisto_main.cpp"}
+PROGRAMS = {"recurgreen": "recurgreen_main.cpp", "plothisto": "plothisto_main.cpp",
+            "waveguide_test": "waveguide_test_main.cpp"}
 SOURCES = ["rg_sweep.cu", "rg_sweep_sym.cu", "rg_sweep_large.cu", "rg_sweep_large_sym.cu", "rg_adjoint.cu",
            "rg_waveguide.cpp", "rg_noalloc.cu", "rg_green.cu", "rg_green.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -85,7 +86,8 @@ def cxx() -> str:
 
 
 def build_programs(force: bool, run) -> None:
-    """bin/recurgreen and bin/plothisto (host C++ over include/recurgreen.hpp)."""
+    """bin/recurgreen, bin/plothisto and bin/waveguide_test (host C++ over
+    include/recurgreen.hpp)."""
     os.makedirs(BIN, exist_ok=True)
     hdrs = [os.path.join(ROOT, "include", "recurgreen.h"), os.path.join(ROOT, "include", "recurgreen.hpp"),
             os.path.join(HOST, "driver.hpp")]

@@ -150,6 +150,9 @@ std::string tag_warn() {
 std::string tag_error() {
   return isatty(STDERR_FILENO) ? "[\033[1m\033[31mERROR\033[0m] " : "[ERROR] ";
 }
+std::string tag_test() {
+  return isatty(STDOUT_FILENO) ? "[\033[1m\033[36mTEST\033[0m] " : "[TEST] ";
+}
 
 NmlGroup read_namelist(const std::string& text, const std::string& name, const std::vector<std::string>& allowed) {
   // Lines without comments (`!` outside quotes).
@@ -885,6 +888,104 @@ int plothisto_main(int argc, char** argv) {
   } catch (const Stop& e) {
     std::fflush(stdout);
     return stop_exit(e.what());
+  } catch (const recurgreen::Error& e) {
+    std::fflush(stdout);
+    return stop_exit(e.what());
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// waveguide_test (src/waveguide.test.f90): the reference's physics checks,
+// printed the same way: the parameters of the test guide, the unitarity
+// defect ||t^H t + r^H r - 1|| of versions 1 and 2 (test_unitarity,
+// src/waveguide.f90:561-590) and ||r_v1 - r_v2||, ||t_v1 - t_v2||
+// (test_green_v1_v2, src/waveguide.f90:598-623), for seeds 1..5.
+// ---------------------------------------------------------------------------
+namespace {
+
+using cvec = std::vector<std::complex<double>>;
+
+// norm2_complex (src/base_utils.f90:208-229): the Frobenius norm.
+double norm2(const cvec& a) {
+  double s = 0.0;
+  for (const auto& z : a) s += std::norm(z);
+  return std::sqrt(s);
+}
+
+// ||t^H t + r^H r - 1|| for nmu x nmu column-major t and r.
+double unitarity_defect(const cvec& t, const cvec& r, int n) {
+  cvec d((size_t)n * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      std::complex<double> s = (i == j) ? -1.0 : 0.0;
+      for (int k = 0; k < n; ++k)
+        s += std::conj(t[(size_t)i * n + k]) * t[(size_t)j * n + k] + std::conj(r[(size_t)i * n + k]) * r[(size_t)j * n + k];
+      d[(size_t)j * n + i] = s;
+    }
+  return norm2(d);
+}
+
+cvec difference(const cvec& a, const cvec& b) {
+  cvec d(a.size());
+  for (size_t e = 0; e < a.size(); ++e) d[e] = a[e] - b[e];
+  return d;
+}
+
+std::string seed_field(int iseed) {  // '(i5)'
+  char buf[16];
+  std::snprintf(buf, sizeof buf, "%5d", iseed);
+  return buf;
+}
+
+recurgreen::Parameters test_guide(int nxdiso, int nxfree) {  // src/waveguide.test.f90:25-39,62-73
+  recurgreen::Parameters p;
+  p.boundtype = "dirichlet";
+  p.wol = 4.30;
+  p.aratio = 1.0;
+  p.exfac = 1.2;
+  p.dscat = 0.2;
+  p.dabso = 0.0;
+  p.napera = 1.0;
+  p.naperb = 1.0;
+  p.nxdiso = nxdiso;
+  p.nxfree = nxfree;
+  return p;
+}
+
+}  // namespace
+
+int waveguide_test_main(int, char**) {
+  try {
+    std::printf("====== TEST INIT_WAVEGUIDE ======\n");
+    {
+      recurgreen::Waveguide w(test_guide(10, 2));
+      w.print_parameters(stdout, "|");
+    }
+    const int nseed = 5;
+    recurgreen::Waveguide w(test_guide(100, 20));
+    const int n = w.get_nmu();
+    cvec r1, t1, r2, t2;
+    for (int version = 1; version <= 2; ++version) {
+      std::printf("====== TEST UNITARITY V%d ======\n", version);
+      if (version == 1) w.print_parameters(stdout, "|");
+      for (int iseed = 1; iseed <= nseed; ++iseed) {
+        if (version == 1) w.compute_refl_trans_v1(iseed, r1, t1);
+        else w.compute_refl_trans_v2(iseed, r1, t1);
+        std::printf("%s#%s | norm(t'*t + r'*r - 1) = %s (expected 0).\n", tag_test().c_str(),
+                    seed_field(iseed).c_str(), format_g0(unitarity_defect(t1, r1, n), 6).c_str());
+      }
+    }
+    std::printf("====== TEST GREEN V1/V2 ======\n");
+    w.print_parameters(stdout, "|");
+    for (int iseed = 1; iseed <= nseed; ++iseed) {
+      w.compute_refl_trans_v1(iseed, r1, t1);
+      w.compute_refl_trans_v2(iseed, r2, t2);
+      std::printf("%s#%s | norm(r_v1 - r_v2) = %s (expected 0).\n", tag_test().c_str(), seed_field(iseed).c_str(),
+                  format_g0(norm2(difference(r1, r2)), 6).c_str());
+      std::printf("%s#%s | norm(t_v1 - t_v2) = %s (expected 0).\n", tag_test().c_str(), seed_field(iseed).c_str(),
+                  format_g0(norm2(difference(t1, t2)), 6).c_str());
+    }
   } catch (const recurgreen::Error& e) {
     std::fflush(stdout);
     return stop_exit(e.what());

@@ -16,6 +16,7 @@ namespace rgdriver {
 std::string tag_info();
 std::string tag_warn();
 std::string tag_error();
+std::string tag_test();
 
 // A stop of the reference's driver: the message goes to stderr, then
 // "RecurGreen: Invalid arguments, aborting..." and a non-zero exit status.
@@ -71,8 +72,10 @@ std::string unique_filename(const std::string& base, const std::string& ext);
 // create_directory (src/base_utils.f90:846-849): mkdir -p.
 void create_directory(const std::string& dir);
 
-// `recurgreen settings.nml ...` and `plothisto settings.nml samples.csv`.
+// `recurgreen settings.nml ...`, `plothisto settings.nml samples.csv` and
+// `waveguide_test` (the reference's src/waveguide.test.f90).
 int recurgreen_main(int argc, char** argv);
 int plothisto_main(int argc, char** argv);
+int waveguide_test_main(int argc, char** argv);
 
 }  // namespace rgdriver

@@ -1,5 +1,6 @@
-"""The C++ host programs bin/recurgreen and bin/plothisto (src/main.f90,
-src/plot_histogram.f90) and the C++ interface include/recurgreen.hpp.
+"""The C++ host programs bin/recurgreen, bin/plothisto and bin/waveguide_test
+(src/main.f90, src/plot_histogram.f90, src/waveguide.test.f90) and the C++
+interface include/recurgreen.hpp.
 
 CPU tests cover everything the programs do before the first GPU call: the
 settings-file checks and their messages, and the Fortran number formats.  GPU
@@ -171,3 +172,21 @@ def test_plothisto_reproduces_reference_replot_fixture(progs, tmp_path):
     assert lines[0] == "%% samples" and lines[1] == "tm, rho"
     assert lines[2:] == r["lines"]
     assert f"Found {len(r['samples'])} samples in the data file..." in out
+
+
+@pytest.mark.gpu
+def test_waveguide_test_program(progs, tmp_path):
+    """src/waveguide.test.f90's checks, printed as the reference prints them, all
+    near zero: unitarity of v1 and v2 and v1 - v2 for seeds 1..5."""
+    rc, out, err = run(progs["waveguide_test"], [], tmp_path)
+    assert rc == 0, err
+    lines = out.splitlines()
+    assert lines[1] == "| Waveguide 2D with boundtype='dirichlet', W/lambda=4.300000, exfac=1.200000, Nmode=10, Nprop=8"
+    heads = [l for l in lines if l.startswith("======")]
+    assert heads == ["====== TEST INIT_WAVEGUIDE ======", "====== TEST UNITARITY V1 ======",
+                     "====== TEST UNITARITY V2 ======", "====== TEST GREEN V1/V2 ======"]
+    tests = [l for l in lines if l.startswith("[TEST] #")]
+    assert len(tests) == 20
+    assert tests[0].startswith("[TEST] #    1 | norm(t'*t + r'*r - 1) = ") and tests[0].endswith(" (expected 0).")
+    for l in tests:
+        assert float(l.split(" = ")[1].split(" (")[0]) < 1e-10, l
