@@ -79,6 +79,7 @@ def lib() -> C.CDLL:
     L.orc_get_meshes.argtypes = [vp, dp, dp]
     L.orc_solve_block_tridiag.argtypes = [vp, dp, vp, C.c_int, vp]
     L.orc_block_tridiag.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]
+    L.orc_amat.argtypes = [vp, dp, C.c_int, vp]
     path, prefix = _find_openblas()
     rc = L.orc_load_lapack(path.encode(), prefix.encode())
     if rc:
@@ -174,6 +175,14 @@ class Waveguide:
         y = np.zeros(self.ny, np.float64)
         lib().orc_get_meshes(self._h, _dp(x), _dp(y))
         return x, y
+
+    def amat_upot(self, upot: np.ndarray, ix: int) -> np.ndarray:
+        """The diagonal block of slice ix (0-based), set_hamiltonian_waveguide
+        (src/waveguide.f90:349-384)."""
+        upot = np.ascontiguousarray(upot, np.float64)
+        a = np.zeros((self.nmu, self.nmu), np.complex128)  # column-major buffer
+        lib().orc_amat(self._h, _dp(upot), ix, a.ctypes.data)
+        return a.T.copy()
 
     def solve_block_tridiag_upot(self, upot: np.ndarray, ind: np.ndarray) -> np.ndarray:
         """solve_block_tridiag (src/base_utils.f90:296-335) on this guide's

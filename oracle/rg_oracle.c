@@ -642,6 +642,14 @@ done:
   return rc;
 }
 
+/* The diagonal block A_ix - V_ix of slice ix (0-based) for potential upot,
+ * nmu x nmu column-major (set_hamiltonian_waveguide, src/waveguide.f90:349-384). */
+void orc_amat(const orc_wg* w, const double* upot, int ix, cplx* amat) {
+  cplx* work = (cplx*)malloc(sizeof(cplx) * ((size_t)w->ny * w->nmu + (size_t)w->nmu * w->nmu));
+  slice_matrix(w, upot, ix, amat, work);
+  free(work);
+}
+
 /* solve_block_tridiag on the waveguide's blocks: amat of
  * set_hamiltonian_waveguide (src/waveguide.f90:349-384) for potential upot,
  * B = bmat, independent term `ind` of nx blocks nmu x k. */

@@ -78,6 +78,29 @@ def test_oracle_full_green_equals_v1(bt, wol):
     np.testing.assert_allclose(r1, r2, atol=1e-13)
 
 
+@pytest.mark.parametrize("bt,wol", [("dirichlet", 2.7), ("periodic", 2.6)])
+def test_oracle_full_green_equals_dense_inverse(bt, wol):
+    """The oracle's solve on the guide's own blocks against numpy's inverse of
+    the assembled block tridiagonal matrix (diagonal blocks A_n - V_n,
+    off-diagonal blocks B), for sources at the first, an inner and the last
+    slice: the general-source solve behind the deposition and wavefunction."""
+    o = O.Waveguide(bt, nxdiso=24, nxfree=2, wol=wol, dscat=2.0, dabso=0.2)
+    u = o.potential(6)
+    M, nx = o.nmu, o.nx
+    b = o.tables()["bmat"]
+    H = np.zeros((nx * M, nx * M), np.complex128)
+    for n in range(nx):
+        H[n * M:(n + 1) * M, n * M:(n + 1) * M] = o.amat_upot(u, n)
+        if n + 1 < nx:
+            H[n * M:(n + 1) * M, (n + 1) * M:(n + 2) * M] = np.diag(b)
+            H[(n + 1) * M:(n + 2) * M, n * M:(n + 1) * M] = np.diag(b)
+    G = np.linalg.inv(H)
+    for ipos in (1, 11, nx):
+        g = o._green(u, ipos)
+        want = G[:, (ipos - 1) * M:ipos * M].reshape(nx, M, M)
+        assert np.max(np.abs(g - want)) <= 1e-11 * np.max(np.abs(want)), ipos
+
+
 def test_oracle_reciprocity_of_deposition():
     """Dirichlet blocks are complex symmetric, so G(x_f; x_i) = G(x_i; x_f)^T."""
     w = O.Waveguide("dirichlet", nxdiso=40, nxfree=1, wol=2.7, dscat=1.5)
