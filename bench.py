@@ -36,7 +36,8 @@ cannot be built here.
          eigenstate profiles for 0.9 <= T <= 1 (compute_tprofile) of --batch
          realizations (default 304) through rg_tprofile_batch, against
          per-realization rg_compute_tprofile calls and the oracle's
-         solve_block_tridiag + zgesvd path on one host core.
+         solve_block_tridiag + zgesvd path on one host core (--wol changes
+         the guide's width: M = floor(2 wol) modes on ny = 4M points).
 """
 from __future__ import annotations
 
@@ -309,6 +310,8 @@ def run_workload(args) -> None:
         import oracle as O
 
         kw = dict(WORKLOAD, nxdiso=args.nx)
+        if args.wol:
+            kw.update(wol=args.wol, ny=4 * int(2 * args.wol))  # M = floor(2 wol) modes on a 4M grid
         w = rg.Waveguide(**kw)
         n = args.batch if args.batch != NSEED else 304
         seeds = np.arange(1, n + 1, dtype=np.int32)
@@ -389,6 +392,8 @@ def main() -> None:
                     help="slices (profiling runs only; the workload is Nx=2000)")
     ap.add_argument("--per-sample", type=int, default=4,
                     help="seeds timed through the per-realization drop-in call (0: skip)")
+    ap.add_argument("--wol", type=float, default=0.0,
+                    help="tprofile workload: W/lambda instead of 32.25 (M = floor(2 wol) modes, ny = 4M)")
     ap.add_argument("--workload", default="uniform", choices=["uniform", "n256", "uneven", "diff", "large", "tprofile"])
     args = ap.parse_args()
     if args.impl == "reference":
