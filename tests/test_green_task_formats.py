@@ -116,3 +116,18 @@ def test_wavefunction_task_file(stand_in, tmp_path):
     assert lines[6] == ", ".join(T.fortran_g0(float(v)) for v in data[0])
     assert len(lines) == 6 + data.shape[0]
     assert path.endswith("wavefun/result_1.wavefun.csv")
+
+
+@pytest.mark.parametrize("task,group", [
+    ("tprofile", "&tprofile tmin=0.25, tmax=0.75, nseed=3 /\n"),
+    ("tprofile_group", "&tprofile_group tm = 0.1, 0.4, 0.6, 0.9, dt = 0.1, 0.1, 0.1, 0.1, nseed = 3 /\n"),
+    ("wavefunction", "&wavefunction iseed=1, ipos=1, imode=1 /\n"),
+])
+def test_command_line_dispatches_the_task(stand_in, tmp_path, capsys, task, group):
+    """`python -m recurgreen_gb300.tdistrib settings.nml` runs the task that
+    &settings names (src/main.f90:41-66) and prints the file it wrote."""
+    (tmp_path / "s.nml").write_text(f"&settings task='{task}' /\n" + WG + group)
+    T.main([str(tmp_path / "s.nml"), "--outdir", str(tmp_path / "out")])
+    printed = capsys.readouterr().out.strip()
+    sub = {"tprofile": "tprofile", "tprofile_group": "tprofile_group", "wavefunction": "wavefun"}[task]
+    assert f"/{sub}/result_1." in printed and printed.startswith(str(tmp_path / "out"))
