@@ -227,6 +227,7 @@ extern "C" {
 
 int rg_tprofile_batch(rg_waveguide* w, const int32_t* seeds, int n, int kind, int nprof, const double* a,
                       const double* b, double* profiles, int32_t* nt, double* tavg, int32_t* status) {
+  rg::NvtxRange nvtx_range("rg_tprofile_batch");
   GreenView v{};
   int rc = rg::green_view(w, &v);
   if (rc) return rc;
@@ -398,6 +399,7 @@ int rg_compute_tprofile_group(rg_waveguide* w, int iseed, int nprof, const doubl
 
 int rg_deposition_batch(rg_waveguide* w, const int32_t* seeds, int n, int fpos, int ipos, int col, double* out,
                         int32_t* status) {
+  rg::NvtxRange nvtx_range("rg_deposition_batch");
   GreenView v{};
   int rc = rg::green_view(w, &v);
   if (rc) return rc;
@@ -474,6 +476,7 @@ int rg_compute_deposition(rg_waveguide* w, int iseed, int fpos, int ipos, double
 }
 
 int rg_compute_refl_trans_v2(rg_waveguide* w, int iseed, double* rmat, double* tmat) {
+  rg::NvtxRange nvtx_range("rg_compute_refl_trans_v2");
   GreenView v{};
   int rc = rg::green_view(w, &v);
   if (rc) return rc;
@@ -489,6 +492,7 @@ int rg_compute_refl_trans_v2(rg_waveguide* w, int iseed, double* rmat, double* t
 }
 
 int rg_compute_wavefunction(rg_waveguide* w, int iseed, int ipos, int imode, double* wfundata, int64_t rows) {
+  rg::NvtxRange nvtx_range("rg_compute_wavefunction");
   GreenView v{};
   int rc = rg::green_view(w, &v);
   if (rc) return rc;
@@ -581,6 +585,7 @@ int rg_compute_wavefunction(rg_waveguide* w, int iseed, int ipos, int imode, dou
 
 int rg_sweep_states(rg_waveguide* w, const double* d_upot, int n, double* d_states, double* d_tfilt, double* d_teig,
                     int32_t* d_status, void* stream) {
+  rg::NvtxRange nvtx_range("rg_sweep_states");
   GreenView v{};
   int rc = rg::green_view(w, &v);
   if (rc) return rc;
@@ -602,6 +607,7 @@ int rg_sweep_states(rg_waveguide* w, const double* d_upot, int n, double* d_stat
 }
 
 int rg_diagonalize_ahca(const double* a, int m, int n, double* T, double* U) {
+  rg::NvtxRange nvtx_range("rg_diagonalize_ahca");
   if (!a || !T || !U || m < 1 || n < 1) return rg::fail(RG_ERR_INVALID_ARG, "rg_diagonalize_ahca: invalid argument");
   Arena ar;
   const int64_t es = rg::eigvec_work_stride(m, n);

@@ -890,6 +890,7 @@ int rg_get_modes(const rg_waveguide* w, double* mumesh, double* bmat) {
 }
 
 int rg_compute_tdistrib(rg_waveguide* w, int iseed, double* tallvals, int64_t len) {
+  rg::NvtxRange nvtx_range("rg_compute_tdistrib");
   if (!w || !tallvals) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_tdistrib: NULL argument");
   // Chunk checks of src/waveguide.f90:408-421.
   const int64_t nchunk = len / w->neigv;
@@ -908,6 +909,7 @@ int rg_compute_tdistrib(rg_waveguide* w, int iseed, double* tallvals, int64_t le
 
 int rg_refl_trans_v1_batch(rg_waveguide* w, const int32_t* seeds, int n, double* rmat, double* tmat,
                            int32_t* status) {
+  rg::NvtxRange nvtx_range("rg_refl_trans_v1_batch");
   if (!w || n < 0 || (n > 0 && (!seeds || !tmat)))
     return rg::fail(RG_ERR_INVALID_ARG, "rg_refl_trans_v1_batch: invalid argument");
   if (n == 0) return RG_OK;
@@ -995,6 +997,7 @@ int rg_tdistrib_upot(rg_waveguide* w, const double* upot, double* teigvals, doub
 }
 
 int rg_compute_refl_trans_v1(rg_waveguide* w, int iseed, double* rmat, double* tmat) {
+  rg::NvtxRange nvtx_range("rg_compute_refl_trans_v1");
   if (!w || !tmat) return rg::fail(RG_ERR_INVALID_ARG, "rg_compute_refl_trans_v1: NULL argument");
   const int32_t s = iseed;
   return run_single(w, &s, nullptr, rg::kModeTmat, nullptr, tmat, nullptr, rmat);
@@ -1035,6 +1038,7 @@ int rg_potential(rg_waveguide* w, int iseed, double* upot) {
 
 int rg_tdistrib_batch_device(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tallvals, int32_t* d_status,
                              void* stream) {
+  rg::NvtxRange nvtx_range("rg_tdistrib_batch_device");
   if (!w || !d_seeds || !d_tallvals || !d_status || n < 0)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_batch_device: invalid argument");
   DeviceGuard g(w->device);
@@ -1046,6 +1050,7 @@ int rg_tdistrib_batch_device(rg_waveguide* w, const int32_t* d_seeds, int n, dou
 }
 
 int rg_tdistrib_batch(rg_waveguide* w, const int32_t* seeds, int n, double* tallvals, int32_t* status) {
+  rg::NvtxRange nvtx_range("rg_tdistrib_batch");
   if (!w || (n > 0 && (!seeds || !tallvals)) || n < 0)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_batch: invalid argument");
   if (n == 0) return RG_OK;
@@ -1088,6 +1093,7 @@ int rg_tdistrib_batch(rg_waveguide* w, const int32_t* seeds, int n, double* tall
 
 int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, const int64_t* offsets,
                       double* tallvals, int64_t len, int32_t* status) {
+  rg::NvtxRange nvtx_range("rg_tdistrib_multi");
   if (n < 0 || (n > 0 && (!wgs || !seeds || !offsets || !tallvals)))
     return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_multi: invalid argument");
   if (n == 0) return RG_OK;
@@ -1224,6 +1230,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
 int rg_sweep_segment(rg_waveguide* w, const double* d_upot, int n, int n_begin, int n_end, const double* d_state_in,
                      double* d_state_dump, double* d_state_out, double* d_tfilt, double* d_teig, int32_t* d_status,
                      void* stream) {
+  rg::NvtxRange nvtx_range("rg_sweep_segment");
   if (!w || !d_upot || !d_status || n < 0) return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: invalid argument");
   if (n_begin < 0 || n_end <= n_begin || n_end > w->nx)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_sweep_segment: need 0 <= n_begin < n_end <= nx");
@@ -1257,6 +1264,7 @@ int rg_sweep_segment(rg_waveguide* w, const double* d_upot, int n, int n_begin, 
 
 int rg_adjoint_grad_rows(rg_waveguide* w, const double* d_xbar, int n, double* d_grad, int64_t grad_stride,
                          void* stream) {
+  rg::NvtxRange nvtx_range("rg_adjoint_grad_rows");
   if (!w || !d_xbar || !d_grad || n < 0) return rg::fail(RG_ERR_INVALID_ARG, "rg_adjoint_grad_rows: invalid argument");
   if (w->p.boundtype != RG_BOUND_DIRICHLET)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_adjoint_grad_rows: the adjoint supports Dirichlet guides only");
@@ -1291,6 +1299,7 @@ int rg_last_batch_info(rg_waveguide* w, rg_batch_info* info) {
 }
 
 int rg_histogram(const double* samples, int64_t n, const double* bins, int nbins, double* histo, double* missing) {
+  rg::NvtxRange nvtx_range("rg_histogram");
   if (!bins || !histo || !missing || (n > 0 && !samples) || n < 0)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_histogram: invalid argument");
   if (nbins < 1) return rg::fail(RG_ERR_INVALID_ARG, "Invalid number of bins");
