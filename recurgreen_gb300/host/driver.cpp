@@ -451,8 +451,11 @@ recurgreen::Parameters waveguide_parameters(const std::string& text) {
 
 void task_tdistrib(const std::string& text, const std::string& root) {
   const recurgreen::Parameters p = waveguide_parameters(text);
-  const NmlGroup td = read_namelist(text, "tdistrib", {"nseed", "nbins", "nthreads", "save_eigvals"});
+  // seed0 (optional, default 1): the first seed, so that runs over disjoint
+  // seed ranges add up to one run over their union.
+  const NmlGroup td = read_namelist(text, "tdistrib", {"nseed", "nbins", "nthreads", "save_eigvals", "seed0"});
   const long nseed = nml_int(td, "nseed", 0);
+  const long seed0 = nml_int(td, "seed0", 1);
   const long nbins = nml_int(td, "nbins", 0);
   const long nthreads = nml_int(td, "nthreads", 1);
   const bool save_eigvals = nml_logical(td, "save_eigvals", false);
@@ -465,10 +468,11 @@ void task_tdistrib(const std::string& text, const std::string& root) {
     throw Stop("Invalid number of threads, received " + fmt_int(nthreads) + " expected >0, aborting...");
   if (nseed < 0) throw Stop("Invalid number of seeds, received " + fmt_int(nseed) + " expected >=0, aborting...");
   if (nbins < 1) throw Stop("Invalid number of bins, received " + fmt_int(nbins) + " expected >0, aborting...");
+  if (seed0 < 1) throw Stop("Invalid first seed, received seed0=" + fmt_int(seed0) + ", expected >0, aborting...");
 
   // The seed loop (src/main.f90:134-179) as one batched GPU launch.
   std::vector<int32_t> seeds(nseed);
-  for (long k = 0; k < nseed; ++k) seeds[k] = (int32_t)(k + 1);
+  for (long k = 0; k < nseed; ++k) seeds[k] = (int32_t)(seed0 + k);
   const auto t0 = std::chrono::steady_clock::now();
   std::vector<double> tallvals = nseed > 0 ? w.tdistrib_batch(seeds) : std::vector<double>();
   const double tsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -249,14 +249,20 @@ def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
     With a torch.distributed process group, each rank (one GPU) takes a
     contiguous range of the seeds; the histogram counts are summed over the
     ranks and rank 0 writes the files (see replicas.py).  Other ranks return
-    the same rho and missing values with no file paths."""
+    the same rho and missing values with no file paths.
+
+    The optional key seed0 (default 1, the reference's first seed) starts the
+    seeds at seed0: runs on separate machines over disjoint ranges give
+    eigenvalue files that together are the run over their union."""
     td = settings["tdistrib"]
     w = _waveguide_from(settings["waveguide"])
-    nseed, nbins = int(td["nseed"]), int(td["nbins"])
+    nseed, nbins, seed0 = int(td["nseed"]), int(td["nbins"]), int(td.get("seed0", 1))
+    if seed0 < 1:
+        raise ValueError(f"Invalid first seed, received seed0={seed0}, expected >0, aborting...")
     if group is not None:
-        return _task_tdistrib_replicas(w, td, nseed, nbins, outdir, group)
+        return _task_tdistrib_replicas(w, td, nseed, nbins, outdir, group, seed0)
     t0 = time.perf_counter()
-    tallvals = w.tdistrib_batch(np.arange(1, nseed + 1, dtype=np.int32))
+    tallvals = w.tdistrib_batch(np.arange(seed0, seed0 + nseed, dtype=np.int32))
     tsec = time.perf_counter() - t0
     rho, missing = prepare_distrib(tallvals, nbins)
     ddir = os.path.join(generate_directory(w, outdir), "distrib")
@@ -272,13 +278,14 @@ def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
     return res
 
 
-def _task_tdistrib_replicas(w: Waveguide, td: dict, nseed: int, nbins: int, outdir: str, group) -> dict:
+def _task_tdistrib_replicas(w: Waveguide, td: dict, nseed: int, nbins: int, outdir: str, group,
+                            seed0: int = 1) -> dict:
     import torch.distributed as dist
 
     from . import replicas
 
     rank, world = dist.get_rank(group), dist.get_world_size(group)
-    seeds = replicas.seed_range(rank, world, nseed)
+    seeds = replicas.seed_range(rank, world, nseed) + (seed0 - 1)
     t0 = time.perf_counter()
     local = w.tdistrib_batch(seeds) if seeds.size else np.zeros(0)
     tsec = replicas.max_over_ranks(time.perf_counter() - t0, group)

@@ -190,3 +190,37 @@ def test_waveguide_test_program(progs, tmp_path):
     assert tests[0].startswith("[TEST] #    1 | norm(t'*t + r'*r - 1) = ") and tests[0].endswith(" (expected 0).")
     for l in tests:
         assert float(l.split(" = ")[1].split(" (")[0]) < 1e-10, l
+
+
+@pytest.mark.gpu
+def test_disjoint_seed_ranges_add_up_to_one_run(progs, tmp_path):
+    """&tdistrib seed0 (optional, default 1): runs over seeds 1..10 and 11..20
+    give the eigenvalue files of one run over 1..20, and plothisto on their
+    concatenation reproduces that run's density rows (the replicas-only
+    multi-machine workflow: disjoint seed ranges, merged on the host)."""
+    from recurgreen_gb300 import tdistrib as T
+
+    def settings(nseed, seed0=None):
+        extra = f", seed0 = {seed0}" if seed0 is not None else ""
+        return SETTINGS.replace("nseed = 40", f"nseed = {nseed}{extra}").replace("nbins = 100", "nbins = 16")
+
+    out = {}
+    for name, text in (("all", settings(20)), ("lo", settings(10, 1)), ("hi", settings(10, 11))):
+        d = tmp_path / name
+        d.mkdir()
+        (d / "s.nml").write_text(text)
+        rc, _, err = run(progs["recurgreen"], ["s.nml"], d)
+        assert rc == 0, err
+        ddir = d / "out" / "dscat_5." / "dabso_0." / "wol_5.25" / "dirichlet" / "distrib"
+        out[name] = ((ddir / "result_1.eigvals.csv").read_text().splitlines()[6:],
+                     (ddir / "result_1.distrib.csv").read_text().splitlines()[6:])
+    assert out["lo"][0] + out["hi"][0] == out["all"][0]
+    merged = tmp_path / "merged.csv"
+    merged.write_text("%% seeds 1..10 and 11..20\n" + "\n".join(out["lo"][0] + out["hi"][0]) + "\n")
+    (tmp_path / "p.nml").write_text("&settings\n bintype = 'chebyshev'\n nbins = 16\n xmin = 0.0\n xmax = 1.0\n/\n")
+    rc, _, err = run(progs["plothisto"], ["p.nml", "merged.csv"], tmp_path)
+    assert rc == 0, err
+    assert (tmp_path / "replot_1.distrib.csv").read_text().splitlines()[2:] == out["all"][1]
+    # the Python driver takes the same key
+    res = T.task_tdistrib(T.read_namelists(settings(10, 11)), str(tmp_path / "py"))
+    assert [T.fortran_g0(float(v)) for v in res["tallvals"]] == out["hi"][0]
