@@ -1,47 +1,49 @@
 """Throughput benchmark of the batched recursive Green sweep on one GB300.
 
-Workload (the batched-uniform configuration): Dirichlet waveguide, W = 1,
-kW/pi = 64.5 (wol = 32.25, M = N = 64 modes), L/W = 1, Nx = 2000 slices,
-L/l_s = 10, eps = 0, U iid normal on a 2000 x 256 grid, seeds 1..4096, one
-realization per seed.  A step is one persistent launch over the whole batch
-(potential generation + sweep + Fisher-Lee + eigenvalues of t^H t); its
-working set (4096 potentials, 16.8 GB) is far larger than L2, so no L2 flush
-is needed between steps.
+Default workload (the metric's configuration, `--workload n256`): Dirichlet
+waveguide, W = 1, kW/pi = 256.5 (wol = 128.25, M = N = 256 modes), L/W = 1,
+Nx = 2000 slices, ny = 1024 transverse points, L/l_s = 10, eps = 0, U iid
+normal drawn from each realization's seed.  A step is one batched call over
+--batch realizations (seeds 1..B): potential generation, the sweep,
+Fisher-Lee and the eigenvalues of t^H t, all inside one persistent launch
+(plus the pivoted re-run of flagged items in the same CUDA graph).
 
-Metric: realizations/s (higher is better).  `value` is device-timed with the
-seeds already in HBM; `e2e` goes through the C ABI with host buffers
-(seeds copied in, eigenvalues and statuses copied out, inside the timing).
-
-`per_realization` times the drop-in path on a few of the same seeds: one
-rg_compute_tdistrib call per seed (the reference's unit of work,
-src/main.f90:156), so `batched_over_per_realization` is the batching gain.
+Metric: realizations/s (higher is better).  The timed loop makes K calls of
+rg_tdistrib_batch, the C-ABI entry point a user calls, with host buffers
+(seeds in, eigenvalues and statuses out):
+  * `value`  = realizations / the summed device time of the K batches (CUDA
+               events recorded by the library around each batch's graph on
+               its launching stream; inputs are already in HBM there);
+  * `e2e`    = realizations / the host wall time of the same K calls
+               (host-to-device and device-to-host copies included).
+`per_realization` times the drop-in path (rg_compute_tdistrib, one call per
+seed, the reference's unit of work, src/main.f90:156) on the same guide, so
+`batched_over_per_realization` is the batching gain the metric names.
 
 `--impl reference` times the reference's CPU algorithm (the oracle's C
-restatement with LAPACK, OpenMP over seeds) on all host cores, on a bounded
-sample of the same workload; gfortran is absent so the Fortran program itself
-cannot be built here.
+restatement with LAPACK, OpenMP over seeds, one seed per host core) on a
+bounded sample of the same workload; gfortran is absent, so the Fortran
+program itself cannot be built.
 
-`--workload` selects a secondary measurement instead of the default line:
-  n256   M=256 modes (kW/pi=256.5, wol=128.25), Nx=2000, ny=1024: batched
-         (--batch realizations, default 152) vs per-realization calls;
-  uneven 2048 guides with N in {32,...,256}, Nx in [500,5000], L/l_s in
-         [1,20], absorption on half (numpy default_rng(0)), ny=4N, through
-         rg_tdistrib_multi, plus per-N histograms;
-  diff   M=128, Nx=1000, ny=512, 256 realizations: Tr(t^H t), Tr((t^H t)^2)
-         and both gradients w.r.t. U through the adjoint sweep (both
-         cotangent chains in one reverse sweep);
-  large  M=512, Nx=10^4 (or --nx, then also extrapolated to 10^4 by slice
-         count), ny=2048, --batch realizations (default 152, one wave);
-  tprofile  the default guide (M=64, Nx=2000, ny=256, L/l_s=10): transmission-
-         eigenstate profiles for 0.9 <= T <= 1 (compute_tprofile) of --batch
-         realizations (default 304) through rg_tprofile_batch, against
-         per-realization rg_compute_tprofile calls and the oracle's
-         solve_block_tridiag + zgesvd path on one host core (--wol changes
-         the guide's width: M = floor(2 wol) modes on ny = 4M points).
+Secondary workloads (`--workload`, one JSON line each, clocks sampled):
+  uniform  the batched-uniform configuration through the same timed loop:
+           M=64 (kW/pi=64.5), Nx=2000, ny=256, seeds 1..4096 per step;
+  uneven   2048 guides with N in {32,...,256}, Nx in [500,5000], L/l_s in
+           [1,20], absorption on half (numpy default_rng(0)), ny=4N, through
+           rg_tdistrib_multi, plus per-N histograms;
+  diff     M=128, Nx=1000, ny=512, 256 realizations: Tr(t^H t), Tr((t^H t)^2)
+           and both gradients w.r.t. U through the adjoint sweep;
+  large    M=512, Nx=10^4 (or --nx), ny=2048, L/l_s=20, --batch
+           realizations (default 152, one wave);
+  tprofile the batched-uniform guide (M=64, Nx=2000, ny=256): transmission-
+           eigenstate profiles for 0.9 <= T <= 1 of --batch realizations;
+  probe    pipe rates (rg_probe_rate: FP64 FMA, FP64 mma.sync, FP16 mma.sync,
+           FP32 FMA) beside cuBLAS DGEMM 8192^3.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -49,31 +51,40 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=32.25, exfac=1.0, aratio=1.0, dscat=10.0,
-                dabso=0.0, napera=1.0, naperb=1.0, ny=256)
-NSEED = 4096
 METRIC = "realizations/s, N=256: batched vs per-realization FP64 GPU, t rel err≤1e-10"
 UNIT = "realizations/s"
 
+BASE = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=128.25, exfac=1.0, aratio=1.0, dscat=10.0,
+            dabso=0.0, napera=1.0, naperb=1.0, ny=1024)
+
+# The timed workloads: waveguide parameters, realizations per step, and the
+# slices of the reference arm's per-step sample.
+SPECS = {
+    "n256": dict(kw=dict(BASE), batch=76, ref_nx=200,
+                 desc="batched N=256: Dirichlet, kW/pi=256.5 (wol=128.25, M=N=256 modes), L/W=1, Nx=2000, "
+                      "ny=1024, L/l_s=10, eps=0"),
+    "uniform": dict(kw=dict(BASE, wol=32.25, ny=256), batch=4096, ref_nx=2000,
+                    desc="batched-uniform: M=64 modes (kW/pi=64.5), Nx=2000, ny=256, L/l_s=10, eps=0"),
+}
+
 
 def flops_per_realization(M: int, nx: int) -> float:
-    """FP64 flops of the reference's slice solve (src/waveguide.f90:426-440):
+    """Algorithmic FP64 flops of the reference's sweep (src/waveguide.f90:426-440):
     16 M^3 per slice (complex inverse 8 M^3 + complex product 8 M^3) for
-    slices 2..Nx plus 8 M^3 for the first inverse.  The pivoted kernel's
+    slices 2..Nx plus 8 M^3 for the first inverse.  The pivoted kernels'
     Gauss-Jordan on [X | B Gs1] does the same 16 M^3 per slice."""
     return 16.0 * M ** 3 * (nx - 1) + 8.0 * M ** 3
 
 
 def flops_symmetric(M: int, nx: int) -> float:
-    """FP64 flops of the symmetric sweep: per slice, M pivot steps each update
-    the M(M+1)/2 stored elements of W and the M x M elements of B Gs1 with one
-    complex FMA (8 flops): 8 M (M(M+1)/2 + M^2) = 12 M^3 + 4 M^2."""
+    """Executed FP64 flops of the symmetric sweeps: per slice, M pivot steps each
+    update the M(M+1)/2 stored elements of W and the M x M elements of B Gs1
+    with one complex FMA (8 flops): 8 M (M(M+1)/2 + M^2) = 12 M^3 + 4 M^2."""
     return (12.0 * M ** 3 + 4.0 * M ** 2) * nx
 
 
@@ -81,12 +92,14 @@ KERNEL_NAMES = {"symmetric": "sweep_sym_kernel<64,256,2>", "pivoted": "sweep_ker
                 "blocked": "sweep_large_kernel", "blocked_symmetric": "sweep_large_sym_kernel"}
 
 
-def config(batch: int) -> dict:
-    nx = WORKLOAD["nxdiso"]
-    return {"workload": f"batched-uniform: M=64 modes (kW/pi=64.5), Nx={nx}, ny=256, L/l_s=10, eps=0, "
-                        f"{batch} realizations (seeds 1..{batch})",
-            "modes": 64, "nx": nx, "ny": 256, "realizations_per_step": batch,
-            "l2": "working set (potentials) 16.8 GB >> L2; no flush needed"}
+def config(spec: dict, batch: int, M: int) -> dict:
+    kw = spec["kw"]
+    ws_mb = 3 * M * M * 16 / 2 ** 20
+    return {"workload": f"{spec['desc']}, {batch} realizations per step (seeds 1..{batch})",
+            "modes": M, "nx": kw["nxdiso"], "ny": kw["ny"], "realizations_per_step": batch,
+            "l2": f"inputs larger than L2: each step draws {batch} potentials of {kw['nxdiso']}x{kw['ny']} "
+                  f"doubles in-kernel ({batch * kw['nxdiso'] * kw['ny'] * 8 / 1e9:.1f} GB if materialised) and "
+                  f"sweeps {ws_mb:.2f} MB of slice matrices per realization; no flush needed"}
 
 
 class ClockSampler:
@@ -107,6 +120,7 @@ class ClockSampler:
                                           "-i", "0", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+        return self
 
     def stop(self) -> dict | None:
         if self.proc is None:
@@ -157,45 +171,57 @@ def measured_fp64_peak(torch) -> tuple[float, str]:
     return 2.0 * 8192 ** 3 / best / 1e12, "cuBLAS DGEMM 8192^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"
 
 
-def cpu_baseline(sample: int, threads: int) -> dict:
+def _ref_sample(spec: dict, threads: int, ref_nx: int):
+    """The reference arm's bounded sample: one seed per host core (seeds
+    1..threads), each sweeping a guide of ref_nx slices with every other
+    parameter of the workload (the per-slice work -- projection, inverse,
+    product -- is the workload's), so a sample is worth threads * ref_nx / Nx
+    realizations of the workload."""
     import oracle as O
 
-    w = O.Waveguide(**WORKLOAD)
-    seeds = list(range(1, sample + 1))
+    nx = spec["kw"]["nxdiso"]
+    w = O.Waveguide(**dict(spec["kw"], nxdiso=min(ref_nx, nx)))
+    seeds = list(range(1, threads + 1))
+    worth = threads * min(ref_nx, nx) / nx
+    desc = (f"{threads} seeds (1..{threads}, one per core) each sweeping the first {min(ref_nx, nx)} of the "
+            f"{nx} slices with the workload's modes and grid, counted as {worth:g} realizations; the "
+            "reference's algorithm restated in C with zgetrf/zgetri/zgesvd/zgemm from OpenBLAS "
+            "(1 BLAS thread per worker); the per-sample zgesvd is included")
+    return w, seeds, worth, desc
+
+
+def cpu_baseline(spec: dict, threads: int, ref_nx: int) -> dict:
+    w, seeds, worth, desc = _ref_sample(spec, threads, ref_nx)
     t0 = time.perf_counter()
     w.tdistrib_batch(seeds, nthreads=threads)
     dt = time.perf_counter() - t0
-    return {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{sample} realizations (seeds 1..{sample}) of the same workload, OpenMP over seeds, "
-                      f"OpenBLAS 1 thread per worker; {dt:.1f} s"}
+    return {"value": worth / dt, "unit": UNIT, "cores": threads, "kind": "port", "sample": f"{desc}; {dt:.1f} s"}
 
 
-def run_reference(args) -> None:
+def run_reference(args, spec: dict) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = args.ref_sample
-    import oracle as O
-
-    w = O.Waveguide(**WORKLOAD)
-    seeds = list(range(1, sample + 1))
+    ref_nx = args.ref_nx or spec["ref_nx"]
+    w, seeds, worth, desc = _ref_sample(spec, threads, ref_nx)
     for _ in range(args.warmup):
-        w.tdistrib_batch(seeds[: max(threads, 1)], nthreads=threads)
+        w.tdistrib_batch(seeds, nthreads=threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         w.tdistrib_batch(seeds, nthreads=threads)
         times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = sample * args.steps / tot
+    value = worth * args.steps / tot
+    M = int(2 * spec["kw"]["wol"])
+    batch = args.batch or spec["batch"]
     out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": config(sample),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded potentials)", "config": config(spec, batch, M),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"{sample} realizations per step (seeds 1..{sample}); the reference's "
-                                      "algorithm restated in C with zgetrf/zgetri/zgesvd/zgemm from OpenBLAS"},
+                            "sample": "each step: " + desc},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -210,8 +236,6 @@ def _sync_time(torch, fn):
 
 def _per_realization(L, w, seeds, np) -> tuple[float, float]:
     """Drop-in path: one rg_compute_tdistrib call per seed; (realizations/s, seconds)."""
-    import ctypes
-
     tall = np.zeros(max(seeds) * w.neigv)
     dp = ctypes.POINTER(ctypes.c_double)
     t0 = time.perf_counter()
@@ -223,10 +247,122 @@ def _per_realization(L, w, seeds, np) -> tuple[float, float]:
     return len(seeds) / dt, dt
 
 
+def run_main(args, spec: dict) -> None:
+    """The timed batched path: K host-buffer rg_tdistrib_batch calls."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import recurgreen_gb300 as rg
+    from recurgreen_gb300 import replicas
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)  # before the NCCL group, which binds to the current device
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.init()
+
+    kw = dict(spec["kw"])
+    if args.nx:
+        kw["nxdiso"] = args.nx
+    spec = dict(spec, kw=kw)
+    w = rg.Waveguide(**kw)
+    n = args.batch or spec["batch"]
+    L = rg.lib()
+    # Replicas: rank r takes seeds r*n+1 .. (r+1)*n (realizations are independent).
+    seeds_h = np.arange(rank * n + 1, (rank + 1) * n + 1, dtype=np.int32)
+    tall = np.zeros(n * w.neigv)
+    status = np.zeros(n, np.int32)
+    ip = ctypes.POINTER(ctypes.c_int32)
+    dp = ctypes.POINTER(ctypes.c_double)
+    fms = ctypes.c_float()
+
+    def step() -> float:
+        rc = L.rg_tdistrib_batch(w._h, seeds_h.ctypes.data_as(ip), n, tall.ctypes.data_as(dp),
+                                 status.ctypes.data_as(ip))
+        if rc:
+            raise rg.RecurGreenError(rc, L.rg_last_error().decode())
+        rc = L.rg_last_sweep_time(w._h, ctypes.byref(fms))
+        if rc:
+            raise rg.RecurGreenError(rc, L.rg_last_error().decode())
+        return fms.value / 1e3
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = ClockSampler().start()
+    torch.cuda.synchronize()
+    sweep_s = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sweep_s.append(step())
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    dev = sum(sweep_s)
+    if world > 1:
+        dev = replicas.max_over_ranks(dev)
+        wall = replicas.max_over_ranks(wall)
+        dist.barrier()
+    bad = int((status != 0).sum())
+    info = w.last_batch_info()
+    M = w.nmu
+    fl = flops_per_realization(M, w.nx)
+    if info["kernel"] in ("symmetric", "blocked_symmetric"):  # re-run items also cost a pivoted sweep
+        fl_exec = flops_symmetric(M, w.nx) + fl * info["rerun"] / n
+    else:
+        fl_exec = fl
+    value = world * n * args.steps / dev
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dev / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potentials)",
+           "config": config(spec, n, M),
+           "timing": "value: summed CUDA-event device time of the K batches (events recorded around each "
+                     "batch's graph on its launching stream); e2e: host wall time of the same K "
+                     "rg_tdistrib_batch calls with host buffers",
+           "e2e": {"value": world * n * args.steps / wall, "unit": UNIT, "h2d_bytes_per_step": 4 * n,
+                   "d2h_bytes_per_step": 8 * n * w.neigv + 4 * n},
+           # this library's kernels per step: the sweep, plus the pivoted re-run
+           # that follows a symmetric sweep in the same graph (empty when nothing is flagged)
+           "gpu_launches": args.steps * (2 if info["kernel"] in ("symmetric", "blocked_symmetric") else 1),
+           "bad_status": bad}
+    if rank == 0:
+        peak, peak_src = measured_fp64_peak(torch)
+        per_launch = sum(sweep_s) / len(sweep_s)  # this rank's batches
+        achieved = fl * n / per_launch / 1e12
+        out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                           "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                           "algorithmic_flops_per_launch": fl * n,
+                           "algorithmic_count": "16 M^3 per slice-solve (slices 2..Nx) + 8 M^3, per realization",
+                           "executed_flops_per_launch": fl_exec * n,
+                           "executed_tflops": fl_exec * n / per_launch / 1e12,
+                           "executed_frac": fl_exec * n / per_launch / 1e12 / peak,
+                           "kernel": KERNEL_NAMES.get(info["kernel"], info["kernel"]), "launch": info,
+                           "kernel_ms_per_launch": 1e3 * per_launch,
+                           "kernel_timing": "CUDA events around each batch's graph (sweep + pivoted re-run)"}
+        out["slice_solves_per_s"] = value * w.nx
+        if args.per_sample > 0:
+            pr, pdt = _per_realization(L, w, list(seeds_h[: args.per_sample]), np)
+            out["per_realization"] = {
+                "value": pr, "unit": UNIT,
+                "sample": f"seeds {int(seeds_h[0])}..{int(seeds_h[min(args.per_sample, n) - 1])}, one "
+                          f"rg_compute_tdistrib call each (host buffers), {pdt:.1f} s"}
+            out["batched_over_per_realization"] = value / pr
+        if clocks:
+            out["clocks"] = clocks
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(spec, os.cpu_count() or 1, args.ref_nx or spec["ref_nx"])
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def run_workload(args) -> None:
     """Secondary measurements (one JSON line each); see the module docstring."""
-    import ctypes
-
     import numpy as np
     import torch
 
@@ -238,36 +374,45 @@ def run_workload(args) -> None:
     peak, peak_src = measured_fp64_peak(torch)
     out["fp64_peak_tflops"] = peak
     out["fp64_peak_source"] = peak_src
-    if args.workload in ("n256", "large"):
-        if args.workload == "n256":
-            kw = dict(WORKLOAD, wol=128.25, nxdiso=args.nx, ny=1024)
-            n = args.batch if args.batch != NSEED else 152
-        else:
-            kw = dict(WORKLOAD, wol=256.25, nxdiso=args.nx if args.nx != 2000 else 10000, dscat=20.0, ny=2048)
-            n = args.batch if args.batch != NSEED else 152
+    clk = ClockSampler()
+    if args.workload == "probe":
+        # the denominators of the roofline: pipe rates from register-only probes
+        names = {0: ("fp64_fma", 100000), 1: ("fp64_mma_m8n8k4", 20000), 2: ("fp64_mma_m16n8k16", 3000),
+                 3: ("fp16_mma_m16n8k16_f32acc", 100000), 4: ("fp32_fma", 1000000)}
+        clk.start()
+        rates = {}
+        for kind, (name, iters) in names.items():
+            v = ctypes.c_double()
+            rc = L.rg_probe_rate(kind, iters, ctypes.byref(v))
+            if rc:
+                raise rg.RecurGreenError(rc, L.rg_last_error().decode())
+            rates[name] = v.value
+        out["clocks"] = clk.stop()
+        out["tflops"] = rates
+        out["tflops"]["cublas_dgemm_8192"] = peak
+        out.pop("fp64_peak_tflops")
+    elif args.workload == "large":
+        kw = dict(BASE, wol=256.25, nxdiso=args.nx or 10000, dscat=20.0, ny=2048)
+        n = args.batch or 152
         w = rg.Waveguide(**kw)
         seeds = np.arange(1, n + 1, dtype=np.int32)
         # warm-up: the autotuner's choice depends on (modes, ny, batch size), not on
         # Nx, so a 16-slice copy of the guide tunes this batch outside the timing
         rg.Waveguide(**dict(kw, nxdiso=16)).tdistrib_batch(seeds)
-        times = []
-        for _ in range(max(args.steps, 1)):
-            dt, _ = _sync_time(torch, lambda: w.tdistrib_batch(seeds))
-            times.append(dt)
+        clk.start()
+        dt, T = _sync_time(torch, lambda: w.tdistrib_batch(seeds))
+        out["clocks"] = clk.stop()
         ms = ctypes.c_float()
         L.rg_last_sweep_time(w._h, ctypes.byref(ms))
         info = w.last_batch_info()
-        dt = min(times)
         fl = flops_per_realization(w.nmu, w.nx)
         out.update({"modes": w.nmu, "nx": w.nx, "ny": w.ny, "realizations": n, "launch": info,
                     "batched_realizations_per_s": n / dt, "batched_seconds": dt,
                     "sweep_kernel_seconds": ms.value / 1e3,
                     "dense_equivalent_tflops": fl * n / (ms.value / 1e3) / 1e12})
         out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
-        if args.workload == "large" and w.nx != 10000:
-            # the sweep time is linear in Nx; the per-realization epilogue is
-            # below 1 % of a 10^4-slice guide at these sizes
-            out["extrapolated_realizations_per_s_at_nx_10000"] = out["batched_realizations_per_s"] * w.nx / 10000
+        T = T.reshape(n, w.neigv)
+        out["smallest_T"] = float(T.min())
         if args.per_sample > 0:
             pr, pdt = _per_realization(L, w, list(range(1, args.per_sample + 1)), np)
             out["per_realization_per_s"] = pr
@@ -276,7 +421,7 @@ def run_workload(args) -> None:
     elif args.workload == "uneven":
         rng = np.random.default_rng(0)
         Ns = [32, 48, 64, 96, 128, 192, 256]
-        n = args.batch if args.batch != NSEED else 2048
+        n = args.batch or 2048
         guides, items, fl = {}, [], 0.0
         t0 = time.perf_counter()
         for k in range(n):
@@ -291,7 +436,9 @@ def run_workload(args) -> None:
             items.append((g, k + 1))
             fl += flops_per_realization(g.nmu, nx)
         t_init = time.perf_counter() - t0
+        clk.start()
         dt, (res, st) = _sync_time(torch, lambda: rg.tdistrib_multi(items, return_status=True))
+        out["clocks"] = clk.stop()
         # per-N histograms of T on the tdistrib task's Chebyshev edges (src/main.f90:233)
         from recurgreen_gb300.tdistrib import chebyshev_bins
         t1 = time.perf_counter()
@@ -309,18 +456,16 @@ def run_workload(args) -> None:
     elif args.workload == "tprofile":
         import oracle as O
 
-        kw = dict(WORKLOAD, nxdiso=args.nx)
+        kw = dict(SPECS["uniform"]["kw"], nxdiso=args.nx or 2000)
         if args.wol:
             kw.update(wol=args.wol, ny=4 * int(2 * args.wol))  # M = floor(2 wol) modes on a 4M grid
         w = rg.Waveguide(**kw)
-        n = args.batch if args.batch != NSEED else 304
+        n = args.batch or 304
         seeds = np.arange(1, n + 1, dtype=np.int32)
         w.tprofile_batch(seeds[:8], "tprofile", [0.9], [1.0])  # warm-up
-        times = []
-        for _ in range(max(args.steps, 1)):
-            dt, (prof, nt, _) = _sync_time(torch, lambda: w.tprofile_batch(seeds, "tprofile", [0.9], [1.0]))
-            times.append(dt)
-        dt = min(times)
+        clk.start()
+        dt, (prof, nt, _) = _sync_time(torch, lambda: w.tprofile_batch(seeds, "tprofile", [0.9], [1.0]))
+        out["clocks"] = clk.stop()
         M, nx = w.nmu, w.nx
         ksel = float(nt.mean())
         fl = flops_per_realization(M, nx) + 16.0 * M * M * ksel * nx  # forward sweep + back-substitution
@@ -348,9 +493,9 @@ def run_workload(args) -> None:
     elif args.workload == "diff":
         from recurgreen_gb300.adjoint import transmission_losses, transmission_losses_and_grads
 
-        kw = dict(WORKLOAD, wol=64.25, nxdiso=args.nx if args.nx != 2000 else 1000, dscat=5.0, ny=512)
+        kw = dict(BASE, wol=64.25, nxdiso=args.nx or 1000, dscat=5.0, ny=512)
         w = rg.Waveguide(**kw)
-        n = args.batch if args.batch != NSEED else 256
+        n = args.batch or 256
         gen = torch.Generator(device="cuda")
         gen.manual_seed(0)
         U = (torch.randn(n, w.nxdiso, w.ny, dtype=torch.float64, device="cuda", generator=gen) * w.stdu)
@@ -365,8 +510,10 @@ def run_workload(args) -> None:
             return g1, g2
 
         fwd()
+        clk.start()
         t_fwd, _ = _sync_time(torch, fwd)
         t_all, (g1, g2) = _sync_time(torch, step)
+        out["clocks"] = clk.stop()
         fl = flops_per_realization(w.nmu, w.nx)
         from recurgreen_gb300.adjoint import _method
         out.update({"adjoint_method": _method(w, U, "auto")})
@@ -384,148 +531,30 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=NSEED)
-    ap.add_argument("--cpu-sample", type=int, default=48)
-    ap.add_argument("--ref-sample", type=int, default=48)
+    ap.add_argument("--batch", type=int, default=0, help="realizations per step (0: the workload's default)")
+    ap.add_argument("--ref-nx", type=int, default=0,
+                    help="slices of each seed of the reference arm's sample (0: the workload's default)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--nx", type=int, default=WORKLOAD["nxdiso"],
-                    help="slices (profiling runs only; the workload is Nx=2000)")
-    ap.add_argument("--per-sample", type=int, default=4,
+    ap.add_argument("--nx", type=int, default=0, help="slices (0: the workload's own; other values for profiling)")
+    ap.add_argument("--per-sample", type=int, default=1,
                     help="seeds timed through the per-realization drop-in call (0: skip)")
     ap.add_argument("--wol", type=float, default=0.0,
                     help="tprofile workload: W/lambda instead of 32.25 (M = floor(2 wol) modes, ny = 4M)")
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "n256", "uneven", "diff", "large", "tprofile"])
+    ap.add_argument("--workload", default="n256",
+                    choices=["n256", "uniform", "uneven", "diff", "large", "tprofile", "probe"])
     args = ap.parse_args()
+    if args.workload in SPECS:
+        spec = SPECS[args.workload]
+        if args.impl == "reference":
+            run_reference(args, spec)
+        else:
+            run_main(args, spec)
+        return
     if args.impl == "reference":
-        WORKLOAD["nxdiso"] = args.nx
-        run_reference(args)
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is defined for the timed "
+                                                              "workloads (n256, uniform) only"}))
         return
-    if args.workload != "uniform":
-        run_workload(args)
-        return
-    WORKLOAD["nxdiso"] = args.nx
-
-    import numpy as np
-    import torch
-    import torch.distributed as dist
-
-    import recurgreen_gb300 as rg
-    from recurgreen_gb300 import replicas
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)  # before the NCCL group, which binds to the current device
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.init()
-
-    w = rg.Waveguide(**WORKLOAD)
-    n = args.batch
-    # Replicas: rank r takes seeds r*n+1 .. (r+1)*n (realizations are independent).
-    seeds_h = np.arange(rank * n + 1, (rank + 1) * n + 1, dtype=np.int32)
-    seeds_d = torch.from_numpy(seeds_h).cuda()
-    out_d = torch.empty(n * w.neigv, dtype=torch.float64, device="cuda")
-    st_d = torch.empty(n, dtype=torch.int32, device="cuda")
-    L = rg.lib()
-    stream = torch.cuda.Stream()  # the library enqueues on this stream; the events below bracket its work
-    stream.wait_stream(torch.cuda.current_stream())
-
-    def device_step():
-        rc = L.rg_tdistrib_batch_device(w._h, seeds_d.data_ptr(), n, out_d.data_ptr(), st_d.data_ptr(),
-                                        stream.cuda_stream)
-        if rc:
-            raise rg.RecurGreenError(rc, L.rg_last_error().decode())
-
-    for _ in range(args.warmup):
-        device_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    clk = ClockSampler()
-    clk.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    sweep_ms = []
-    fms = __import__("ctypes").c_float()
-    e0.record(stream)
-    for _ in range(args.steps):
-        device_step()
-        if L.rg_last_sweep_time(w._h, __import__("ctypes").byref(fms)) == 0:
-            sweep_ms.append(fms.value)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clocks = clk.stop()
-    dt = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        dt = replicas.max_over_ranks(dt)
-        dist.barrier()
-    bad = int((st_d != 0).sum().item())
-
-    # End to end through the C ABI with host buffers.
-    tall = np.zeros(n * w.neigv)
-    status = np.zeros(n, np.int32)
-    ip = __import__("ctypes").POINTER(__import__("ctypes").c_int32)
-    dp = __import__("ctypes").POINTER(__import__("ctypes").c_double)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        rc = L.rg_tdistrib_batch(w._h, seeds_h.ctypes.data_as(ip), n, tall.ctypes.data_as(dp),
-                                 status.ctypes.data_as(ip))
-        if rc:
-            raise rg.RecurGreenError(rc, L.rg_last_error().decode())
-    e2e_dt = time.perf_counter() - t0
-    if world > 1:
-        e2e_dt = replicas.max_over_ranks(e2e_dt)
-    per = None
-    if args.per_sample > 0 and rank == 0:
-        pr, pdt = _per_realization(L, w, list(seeds_h[: args.per_sample]), np)
-        per = {"value": pr, "unit": UNIT,
-               "sample": f"seeds {int(seeds_h[0])}..{int(seeds_h[min(args.per_sample, n) - 1])}, one "
-                         f"rg_compute_tdistrib call each (host buffers, one CTA per call), {pdt:.1f} s"}
-
-    info = w.last_batch_info()
-    fl = flops_per_realization(w.nmu, w.nx)
-    if info["kernel"] == "symmetric":  # re-run items also cost a pivoted sweep
-        fl_exec = flops_symmetric(w.nmu, w.nx) + fl * info["rerun"] / n
-    else:
-        fl_exec = fl
-    value = world * n * args.steps / dt
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potentials)",
-           "config": config(n),
-           "e2e": {"value": world * n * args.steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": 4 * n,
-                   "d2h_bytes_per_step": 8 * n * w.neigv + 4 * n},
-           # this library's kernels per step: the sweep, plus the pivoted re-run
-           # that follows a symmetric sweep in the same graph (empty when nothing is flagged)
-           "gpu_launches": args.steps * (2 if info["kernel"] in ("symmetric", "blocked_symmetric") else 1),
-           "bad_status": bad}
-    if rank == 0:
-        peak, peak_src = measured_fp64_peak(torch)
-        # the sweep kernel's own duration: CUDA events recorded around its
-        # launch inside the library, on the same stream (rg_last_sweep_time)
-        sweep_s = (sum(sweep_ms) / len(sweep_ms) / 1e3) if len(sweep_ms) == args.steps else dt / args.steps
-        achieved = fl_exec * n / sweep_s / 1e12
-        out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                           "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
-                           "algorithmic_flops_per_launch": fl_exec * n,
-                           "kernel": KERNEL_NAMES.get(info["kernel"], info["kernel"]), "launch": info,
-                           "dense_equivalent_tflops": fl * n / sweep_s / 1e12,
-                           "kernel_ms_per_launch": 1e3 * sweep_s,
-                           "kernel_timing": "CUDA events around the sweep launch" if len(sweep_ms) == args.steps
-                           else "whole step (potential + sweep)"}
-        out["slice_solves_per_s"] = value * (w.nx)
-        if per:
-            out["per_realization"] = per
-            out["batched_over_per_realization"] = value / per["value"]
-        if clocks:
-            out["clocks"] = clocks
-        if not args.no_cpu:
-            out["cpu_baseline"] = cpu_baseline(args.cpu_sample, os.cpu_count() or 1)
-        print(json.dumps(out))
-    if world > 1:
-        dist.destroy_process_group()
+    run_workload(args)
 
 
 if __name__ == "__main__":

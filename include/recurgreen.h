@@ -303,6 +303,14 @@ int rg_last_batch_info(rg_waveguide* wg, rg_batch_info* info);
  * Calls that overlap on the GPU race on the shared array. */
 int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_teigvals, int32_t* d_status, void* stream);
 
+/* No counterpart in the reference: throughput of one arithmetic pipe of the
+ * current device, in TFLOP/s, from a full grid of independent dependency
+ * chains on register operands (the denominators of the sweep's roofline).
+ * kind 0: FP64 FMA; 1: FP64 mma.sync m8n8k4; 2: FP64 mma.sync m16n8k16;
+ * 3: FP16 mma.sync m16n8k16 with FP32 accumulation; 4: FP32 FMA.  iters is
+ * the loop count per thread (about 1e5 gives ~0.1 s for kind 0). */
+int rg_probe_rate(int kind, int iters, double* tflops);
+
 /* histogram (src/base_utils.f90:491-516) with the reference's exact edge
  * semantics, computed on the GPU: samples[n] and bins[nbins+1] are host
  * arrays; histo[nbins] and *missing receive counts as doubles. */

@@ -30,7 +30,7 @@ EXPORTS = (
     "rg_adjoint_grad_rows", "rg_get_modes", "rg_last_batch_info", "rg_refl_trans_v1_batch",
     "rg_tprofile_batch", "rg_compute_tprofile", "rg_compute_itx_profile", "rg_compute_tprofile_group",
     "rg_compute_deposition", "rg_deposition_batch", "rg_compute_wavefunction", "rg_diagonalize_ahca",
-    "rg_sweep_states", "rg_compute_refl_trans_v2",
+    "rg_sweep_states", "rg_compute_refl_trans_v2", "rg_probe_rate",
 )
 PROFILE_KINDS = {"tprofile": 0, "itx": 1, "group": 2}
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
@@ -100,6 +100,7 @@ def lib() -> C.CDLL:
     L.rg_diagonalize_ahca.argtypes = [vp, C.c_int, C.c_int, dp, vp]
     L.rg_sweep_states.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp]
     L.rg_compute_refl_trans_v2.argtypes = [vp, C.c_int, vp, vp]
+    L.rg_probe_rate.argtypes = [C.c_int, C.c_int, dp]
     _LIB = L
     return L
 

@@ -26,7 +26,7 @@ HOST_SOURCES = ["driver.cpp"]
 PROGRAMS = {"recurgreen": "recurgreen_main.cpp", "plothisto": "plothisto_main.cpp",
             "waveguide_test": "waveguide_test_main.cpp"}
 SOURCES = ["rg_sweep.cu", "rg_sweep_sym.cu", "rg_sweep_large.cu", "rg_sweep_large_sym.cu", "rg_adjoint.cu",
-           "rg_waveguide.cpp", "rg_noalloc.cu", "rg_green.cu", "rg_green.cpp"]
+           "rg_waveguide.cpp", "rg_noalloc.cu", "rg_green.cu", "rg_green.cpp", "rg_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "-I", os.path.join(ROOT, "include")]

@@ -1,0 +1,125 @@
+"""Full-length parity at the metric's configuration and at 512 modes.
+
+N256: the configuration the metric is quoted on -- Dirichlet, kW/pi = 256.5
+(M = N = 256 modes), Nx = 2000 slices, ny = 1024, L/l_s = 10, eps = 0 --
+for seeds 1 and 2.  The oracle (the reference's algorithm with LAPACK) runs
+here on the same potentials, both seeds in parallel threads (~75 s each on
+one core); the GPU runs the blocked symmetric sweep.
+
+C5 short: 512 modes, ny = 2048, L/l_s = 20 (the large diffusive guide, whose
+smallest eigenvalues are closed channels near exp(-2L/xi)) over 2000 slices,
+seeds 1 and 2, against oracle fixtures made by tests/golden/make_large_fixtures.py
+(the oracle needs ~6 min per seed there).
+
+Bars:
+  * t: relative Frobenius error <= 1e-10 (C5: estimated from a 4-vector
+    Gaussian sketch t @ V, ||D V||_F^2 / K being an unbiased estimate of ||D||_F^2);
+  * T_n: absolute error <= 1e-9;
+  * every T_n, small ones included, within Weyl's bound: the singular values of
+    two matrices differ by at most the 2-norm of their difference, so
+    |sqrt(Tg_n) - sqrt(To_n)| <= ||tg - to||_F plus both sides' SVD backward
+    error (64 eps ||t||_2).  For T_n = 1e-12 and ||tg - to||_F = 1e-13 this
+    is a per-eigenvalue relative bar of 2e-7.
+"""
+import os
+import threading
+
+import numpy as np
+import pytest
+
+import oracle as O
+import recurgreen_gb300 as rg
+
+pytestmark = pytest.mark.gpu
+
+T_REL = 1e-10
+TN_ABS = 1e-9
+EPS = np.finfo(np.float64).eps
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+N256 = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=128.25, exfac=1.0, aratio=1.0, dscat=10.0, ny=1024)
+C5SHORT = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=256.25, exfac=1.0, aratio=1.0, dscat=20.0, ny=2048)
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def weyl_ok(Tg, To, dt_fro, t2norm):
+    """|sqrt(Tg) - sqrt(To)| <= ||tg - to||_F + 64 eps ||t||_2, elementwise."""
+    sg, so = np.sqrt(np.maximum(Tg, 0.0)), np.sqrt(np.maximum(To, 0.0))
+    return np.abs(sg - so) <= dt_fro + 64 * EPS * t2norm
+
+
+@pytest.fixture(scope="module")
+def n256():
+    o = O.Waveguide(**N256)
+    g = rg.Waveguide(**N256)
+    seeds = (1, 2)
+    pots = {s: o.potential(s) for s in seeds}
+    res = {}
+
+    def run(s):
+        res[s] = o.tdistrib_upot(pots[s], want_t=True)
+
+    th = [threading.Thread(target=run, args=(s,)) for s in seeds]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    return o, g, pots, res
+
+
+def test_n256_full_length_upot(n256):
+    o, g, pots, res = n256
+    assert g.nmu == 256 and g.neigv == 256 and g.nx == 2000
+    for s, u in pots.items():
+        To, to = res[s]
+        Tg, tg = g.tdistrib_upot(u, want_t=True)
+        dt = np.linalg.norm(tg - to)
+        assert dt / np.linalg.norm(to) <= T_REL, s
+        assert np.max(np.abs(Tg - To)) <= TN_ABS, s
+        assert np.all(weyl_ok(Tg, To, dt, np.sqrt(To[0]))), s
+        assert np.all(np.diff(Tg) <= 0)
+        assert np.all((Tg >= -1e-12) & (Tg <= 1 + 1e-12))  # dabso = 0: 0 <= T <= 1
+
+
+def test_n256_seed_path_batch(n256):
+    """The seed-driven batched path (potential drawn in the kernel) against the
+    oracle on the oracle's own draw of the same seeds."""
+    o, g, pots, res = n256
+    T = g.tdistrib_batch(np.array([1, 2], np.int32)).reshape(2, g.neigv)
+    for k, s in enumerate((1, 2)):
+        To, to = res[s]
+        assert np.max(np.abs(T[k] - To)) <= TN_ABS, s
+        assert np.all(weyl_ok(T[k], To, T_REL * np.linalg.norm(to), np.sqrt(To[0]))), s
+
+
+def _fixture(name):
+    p = os.path.join(HERE, "golden", f"oracle_{name}.npz")
+    if not os.path.exists(p):
+        pytest.fail(f"missing fixture {p}: run tests/golden/make_large_fixtures.py {name}")
+    return np.load(p)
+
+
+def test_c5short_closed_channels():
+    """512 modes, L/l_s = 20: every eigenvalue, down to the closed channels,
+    against the oracle fixture, within Weyl's bound of the measured t error."""
+    from golden.make_large_fixtures import SKETCH_K, sketch_vectors
+
+    f = _fixture("c5short")
+    g = rg.Waveguide(**C5SHORT)
+    o = O.Waveguide(**C5SHORT)
+    assert g.nmu == 512 and g.nx == 2000
+    for k, s in enumerate(f["seeds"]):
+        To, tn, sk = f["T"][k], float(f["tnorm"][k]), f["sketch"][k]
+        Tg, tg = g.tdistrib_upot(o.potential(int(s)), want_t=True)
+        V = sketch_vectors(tg.shape[1])
+        dt_est = np.linalg.norm(tg @ V - sk) / np.sqrt(SKETCH_K)
+        assert dt_est / tn <= T_REL, s
+        assert abs(np.linalg.norm(tg) - tn) <= T_REL * tn, s
+        assert np.max(np.abs(Tg - To)) <= TN_ABS, s
+        assert To.min() < 1e-10  # the guide does reach closed channels
+        # Weyl with 4x the sketch estimate (a 4-vector estimate is within a
+        # factor 2 of ||D||_F with overwhelming probability)
+        assert np.all(weyl_ok(Tg, To, 4 * dt_est, np.sqrt(To[0]))), s
