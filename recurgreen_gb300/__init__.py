@@ -31,6 +31,7 @@ EXPORTS = (
     "rg_tprofile_batch", "rg_compute_tprofile", "rg_compute_itx_profile", "rg_compute_tprofile_group",
     "rg_compute_deposition", "rg_deposition_batch", "rg_compute_wavefunction", "rg_diagonalize_ahca",
     "rg_sweep_states", "rg_compute_refl_trans_v2", "rg_probe_rate",
+    "rg_ozaki_zgemm",
 )
 PROFILE_KINDS = {"tprofile": 0, "itx": 1, "group": 2}
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
@@ -101,6 +102,7 @@ def lib() -> C.CDLL:
     L.rg_sweep_states.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp]
     L.rg_compute_refl_trans_v2.argtypes = [vp, C.c_int, vp, vp]
     L.rg_probe_rate.argtypes = [C.c_int, C.c_int, dp]
+    L.rg_ozaki_zgemm.argtypes = [C.c_int, vp, vp, vp]
     _LIB = L
     return L
 
@@ -406,6 +408,17 @@ def diagonalize_ahca(a):
     U = np.zeros((n, n), np.complex128, order="F")
     _check(lib().rg_diagonalize_ahca(a.ctypes.data, m, n, _dp(T), U.ctypes.data))
     return T, U
+
+
+def ozaki_zgemm(a, b) -> np.ndarray:
+    """C = A B (complex, M x M) through the tensor-core digit path (rg_ozaki_zgemm)."""
+    a = np.asfortranarray(a, np.complex128)
+    b = np.asfortranarray(b, np.complex128)
+    M = a.shape[0]
+    assert a.shape == (M, M) and b.shape == (M, M)
+    c = np.zeros((M, M), np.complex128, order="F")
+    _check(lib().rg_ozaki_zgemm(M, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+    return c
 
 
 def histogram(samples, bins):

@@ -26,7 +26,7 @@ HOST_SOURCES = ["driver.cpp"]
 PROGRAMS = {"recurgreen": "recurgreen_main.cpp", "plothisto": "plothisto_main.cpp",
             "waveguide_test": "waveguide_test_main.cpp"}
 SOURCES = ["rg_sweep.cu", "rg_sweep_sym.cu", "rg_sweep_large.cu", "rg_sweep_large_sym.cu", "rg_adjoint.cu",
-           "rg_waveguide.cpp", "rg_noalloc.cu", "rg_green.cu", "rg_green.cpp", "rg_probe.cu"]
+           "rg_waveguide.cpp", "rg_noalloc.cu", "rg_green.cu", "rg_green.cpp", "rg_probe.cu", "rg_ozaki.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "-I", os.path.join(ROOT, "include")]
@@ -49,6 +49,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     headers = [os.path.join(CSRC, "rg_internal.h"), os.path.join(CSRC, "rg_device.cuh"),
+               os.path.join(CSRC, "rg_ozaki.cuh"),
                os.path.join(ROOT, "include", "recurgreen.h")]
     jobs = []
     objs = []

@@ -126,6 +126,12 @@ struct SweepArgs {
   // source at slice inject_at (src/base_utils.f90:318-324), zero before it.
   // 0 is the usual sweep (source at slice 0, where Z_0 = Gss_0).
   int inject_at;
+  // 1: the blocked symmetric kernel forms the propagator product Gss (B Gs1)
+  // on the tensor cores (rg_ozaki.cuh) after inverting X on its own, instead
+  // of carrying B Gs1 through the Gauss-Jordan sweep; used when no states
+  // are kept (state_dump == nullptr, inject_at == 0).  Set from RG_TENSOR_R
+  // (default on).
+  int tensor_r;
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were

@@ -1,0 +1,277 @@
+// Complex FP64 matrix products on the FP16 tensor cores (Ozaki splitting).
+//
+// C = A B for M x M complex matrices (M <= 512), computed with mma.sync
+// m16n8k16 (FP16 inputs, FP32 accumulation) to FP64 accuracy:
+//
+//  * every row i of A gets the exponent ea_i of its largest |re| or |im|
+//    (|A_ik| < 2^ea_i), every column j of B the exponent eb_j likewise;
+//  * each entry is written as a 56-bit fixed-point integer relative to that
+//    power of two (rounded to nearest), cut into 8 signed 7-bit digits:
+//        A_ik = 2^ea_i sum_p a_p 2^(-7(p+1)),  |a_p| <= 127,  p = 0..7
+//    (exact in FP16);
+//  * C_ij = 2^(ea_i + eb_j) sum_l 2^(-7(l+2)) v_l with
+//        v_l = sum_{p+q=l} sum_k a_p(i,k) b_q(k,j),
+//    and levels l <= 8 kept (43 digit pairs; the dropped ones lie below
+//    2^-51 relative to 2^(ea_i+eb_j), under an FP64 product's rounding);
+//  * v_l is accumulated in FP32 over chunks of 64 complex k: at most
+//    8 pairs x 128 real products x 127^2 = 16,516,096 < 2^24 per level, so
+//    every partial sum is an integer below 2^24 and the accumulation is
+//    exact; after each chunk the levels are folded into two int64 sums,
+//    hi = sum_{l<=3} v_l 2^(7(3-l)) and lo = sum_{l>=4} v_l 2^(7(8-l)),
+//    which are exact too (|hi| < 2^48, |lo| < 2^55 for M <= 512);
+//  * finally C_ij = 2^(ea_i+eb_j) (hi 2^-35 + lo 2^-70), one rounding.
+//
+// The result is the correctly rounded value of the digit sum, so it does
+// not depend on how tiles are spread over warps or CTAs, and it equals an
+// exact integer model of the same steps bit for bit.  Its error is that of
+// the dropped digit pairs and the 2^-56 rounding of the inputs, i.e.
+// normwise at the level of an FP64 product (2^-53 * K * |A_i| |B_j| at worst).
+//
+// Layouts ("fragment-native", so a lane loads its mma operand with one
+// 16-byte access).  With T = ceil(M/16) tiles per dimension:
+//   A digits  uint4 [2 parts][8 slices][T row tiles][T k tiles][32 lanes]
+//             lane (g = lane/4, t = lane%4) of tile (ti, tk) holds the halves
+//             (A[g][2t], A[g][2t+1]), (A[g+8][2t], A[g+8][2t+1]),
+//             (A[g][2t+8], A[g][2t+9]), (A[g+8][2t+8], A[g+8][2t+9])
+//             of the 16 x 16 tile: the m16n8k16 A fragment (row-major);
+//   B digits  uint4 [2 parts][8 slices][T col tiles][T k tiles][32 lanes]
+//             lane holds (B[2t][g], B[2t+1][g]), (B[2t+8][g], B[2t+9][g]) of
+//             columns 0..7 of the tile, then the same for columns 8..15: two
+//             m16n8k16 B fragments (column-major);
+//   accumulators: c0 = C[g][2t], c1 = C[g][2t+1], c2 = C[g+8][2t], c3 = C[g+8][2t+1].
+// Rows/columns beyond M are zero digits.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace rg {
+namespace oz {
+
+constexpr int kSlices = 8;                 // digits per entry
+constexpr int kLmax = 8;                   // highest level kept
+constexpr int kChunkTiles = 4;             // k tiles (of 16 complex k) per fold
+constexpr int kNoExp = -4096;              // exponent of zero rows
+
+__host__ __device__ inline int tiles(int M) { return (M + 15) >> 4; }
+// uint4 elements of one operand's digits
+__host__ __device__ inline int64_t operand_uint4(int M) {
+  const int64_t T = tiles(M);
+  return 2LL * kSlices * T * T * 32;
+}
+// bytes of both operands' digits plus the exponents (2 x M ints, 16-byte padded)
+__host__ __device__ inline int64_t workspace_bytes(int M) {
+  return 2 * 16 * operand_uint4(M) + (((int64_t)2 * tiles(M) * 16 * 4 + 15) & ~15LL);
+}
+
+// frexp exponent of |x| (|x| < 2^e), kNoExp for zeros and subnormals.
+__device__ __forceinline__ int fexp(double x) {
+  const int eb = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  return eb == 0 ? kNoExp : eb - 1022;
+}
+
+__device__ __forceinline__ int fexp2(double2 v) { return max(fexp(v.x), fexp(v.y)); }
+
+// |x| 2^(56-e) rounded to nearest, as an integer below 2^56 (e >= fexp(x)).
+__device__ __forceinline__ uint64_t fixed56(double x, int e) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0;
+  const uint64_t m = (bits & ((1ULL << 52) - 1)) | (1ULL << 52);
+  const int sh = eb - 1019 - e;  // |x| 2^(56-e) = m 2^sh, sh <= 3
+  if (sh >= 0) return m << sh;
+  const int rs = -sh;
+  if (rs > 54) return 0;
+  return (m + (1ULL << (rs - 1))) >> rs;
+}
+
+// Digits p of two entries packed as two FP16 halves (lo = first).  A digit
+// d in [0, 127] is made exact in FP16 as (1024 + d) - 1024, then signed.
+__device__ __forceinline__ uint32_t digit_pair(uint64_t x0, bool n0, uint64_t x1, bool n1, int p) {
+  const int sh = 49 - 7 * p;
+  const uint32_t d0 = (uint32_t)(x0 >> sh) & 127u, d1 = (uint32_t)(x1 >> sh) & 127u;
+  const uint32_t biased = (0x6400u | d0) | ((0x6400u | d1) << 16);
+  __half2 h;
+  memcpy(&h, &biased, 4);
+  h = __hsub2(h, __floats2half2_rn(1024.0f, 1024.0f));
+  uint32_t r;
+  memcpy(&r, &h, 4);
+  // the sign of a zero digit does not matter (its products are +-0)
+  return r ^ ((n0 ? 0x8000u : 0u) | (n1 ? 0x80000000u : 0u));
+}
+
+// Writes the 16 uint4 (2 parts x 8 slices) of one lane of one tile from its
+// 8 complex entries v[0..7] in fragment order (see the layout above) and
+// the row (A) or column (B) exponents of each entry: for A, entries 0,1,4,5
+// lie on row g and 2,3,6,7 on row g+8; for B, entries 0..3 on column g and
+// 4..7 on column g+8.  dst points at [part 0][slice 0][this tile][lane];
+// `plane` is the uint4 stride between slices.
+__device__ __forceinline__ void write_digits(const double2 v[8], const int e[8], uint4* dst, int64_t plane) {
+  uint64_t xr[8], xi[8];
+  bool nr[8], ni[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    xr[k] = fixed56(v[k].x, e[k]);
+    xi[k] = fixed56(v[k].y, e[k]);
+    nr[k] = v[k].x < 0.0;
+    ni[k] = v[k].y < 0.0;
+  }
+#pragma unroll
+  for (int p = 0; p < kSlices; ++p) {
+    uint4 r, i;
+    r.x = digit_pair(xr[0], nr[0], xr[1], nr[1], p);
+    r.y = digit_pair(xr[2], nr[2], xr[3], nr[3], p);
+    r.z = digit_pair(xr[4], nr[4], xr[5], nr[5], p);
+    r.w = digit_pair(xr[6], nr[6], xr[7], nr[7], p);
+    i.x = digit_pair(xi[0], ni[0], xi[1], ni[1], p);
+    i.y = digit_pair(xi[2], ni[2], xi[3], ni[3], p);
+    i.z = digit_pair(xi[4], ni[4], xi[5], ni[5], p);
+    i.w = digit_pair(xi[6], ni[6], xi[7], ni[7], p);
+    __stcg(dst + p * plane, r);
+    __stcg(dst + (kSlices + p) * plane, i);
+  }
+}
+
+// Digit planes of A: entries A(i, k) = getA(i, k) (zero outside M x M),
+// exponents ea[i].  Task = (row tile, k tile, lane), spread over
+// [task0, ntask) with stride `step`.
+template <class GetA>
+__device__ void split_a(int M, GetA getA, const int* ea, uint4* dig, int task0, int step) {
+  const int T = tiles(M);
+  const int64_t plane = (int64_t)T * T * 32;
+  const int ntask = T * T * 32;
+  for (int task = task0; task < ntask; task += step) {
+    const int lane = task & 31, tk = (task >> 5) % T, ti = (task >> 5) / T;
+    const int g = lane >> 2, t = lane & 3;
+    const int r0 = ti * 16 + g, r1 = r0 + 8;
+    const int cs[4] = {tk * 16 + 2 * t, tk * 16 + 2 * t + 1, tk * 16 + 2 * t + 8, tk * 16 + 2 * t + 9};
+    double2 v[8];
+    int e[8];
+    const int rows[8] = {r0, r0, r1, r1, r0, r0, r1, r1};
+    const int cols[8] = {cs[0], cs[1], cs[0], cs[1], cs[2], cs[3], cs[2], cs[3]};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const bool in = rows[k] < M && cols[k] < M;
+      v[k] = in ? getA(rows[k], cols[k]) : make_double2(0.0, 0.0);
+      e[k] = rows[k] < M ? ea[rows[k]] : 0;
+    }
+    write_digits(v, e, dig + ((int64_t)ti * T + tk) * 32 + lane, plane);
+  }
+}
+
+// Digit planes of B: entries B(k, j) = getB(k, j), exponents eb[j].
+template <class GetB>
+__device__ void split_b(int M, GetB getB, const int* eb, uint4* dig, int task0, int step) {
+  const int T = tiles(M);
+  const int64_t plane = (int64_t)T * T * 32;
+  const int ntask = T * T * 32;
+  for (int task = task0; task < ntask; task += step) {
+    const int lane = task & 31, tk = (task >> 5) % T, tj = (task >> 5) / T;
+    const int g = lane >> 2, t = lane & 3;
+    const int c0 = tj * 16 + g, c1 = c0 + 8;
+    const int ks[4] = {tk * 16 + 2 * t, tk * 16 + 2 * t + 1, tk * 16 + 2 * t + 8, tk * 16 + 2 * t + 9};
+    double2 v[8];
+    int e[8];
+    const int rows[8] = {ks[0], ks[1], ks[2], ks[3], ks[0], ks[1], ks[2], ks[3]};
+    const int cols[8] = {c0, c0, c0, c0, c1, c1, c1, c1};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const bool in = rows[k] < M && cols[k] < M;
+      v[k] = in ? getB(rows[k], cols[k]) : make_double2(0.0, 0.0);
+      e[k] = cols[k] < M ? eb[cols[k]] : 0;
+    }
+    write_digits(v, e, dig + ((int64_t)tj * T + tk) * 32 + lane, plane);
+  }
+}
+
+__device__ __forceinline__ void mma16816(float c[4], const uint4& a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+// One warp's 16 x 16 complex tile (ti, tj) of C = A B over all k.  The A
+// digits of the current chunk come from shared memory (astage: [2][8][4][32]
+// uint4, filled by the caller's stage_a for this row tile and chunk); the B
+// digits are read from global memory (L2).  `stage` is called with the chunk
+// index before the chunk's products and must leave astage filled for every
+// warp (it synchronises the CTA).  out(i, j, re, im) stores C_ij.
+template <class Stage, class Out>
+__device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig, const int* ea, const int* eb,
+                          const uint4* astage, Stage stage, Out out) {
+  const int T = tiles(M);
+  const int lane = threadIdx.x & 31;
+  const int64_t bplane = (int64_t)T * T * 32;
+  long long hi[16], lo[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) hi[k] = lo[k] = 0;
+  const int nchunk = (T + kChunkTiles - 1) / kChunkTiles;
+  for (int ch = 0; ch < nchunk; ++ch) {
+    stage(ch);
+    const int nk = min(kChunkTiles, T - ch * kChunkTiles);
+    if (active) {
+      const uint4* bbase = bdig + ((int64_t)tj * T + ch * kChunkTiles) * 32 + lane;
+#pragma unroll 1
+      for (int l = 0; l <= kLmax; ++l) {
+        float acc[4][4];  // [re n0, re n1, im n0, im n1][4]
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) acc[u][w] = 0.0f;
+        const int p0 = max(0, l - (kSlices - 1)), p1 = min(l, kSlices - 1);
+#pragma unroll 1
+        for (int p = p0; p <= p1; ++p) {
+          const int q = l - p;
+          const uint4* br = bbase + (int64_t)q * bplane;
+          const uint4* bi = bbase + (int64_t)(kSlices + q) * bplane;
+          const uint4* ar = astage + (p * kChunkTiles) * 32 + lane;
+          const uint4* ai = astage + ((kSlices + p) * kChunkTiles) * 32 + lane;
+#pragma unroll
+          for (int kk = 0; kk < kChunkTiles; ++kk) {
+            if (kk < nk) {
+              const uint4 vbr = __ldcg(br + kk * 32), vbi = __ldcg(bi + kk * 32);
+              const uint4 var = ar[kk * 32], vai = ai[kk * 32];
+              // re += Ar Br - Ai Bi; im += Ar Bi + Ai Br
+              mma16816(acc[0], var, vbr.x, vbr.y);
+              mma16816(acc[0], vai, vbi.x ^ 0x80008000u, vbi.y ^ 0x80008000u);
+              mma16816(acc[1], var, vbr.z, vbr.w);
+              mma16816(acc[1], vai, vbi.z ^ 0x80008000u, vbi.w ^ 0x80008000u);
+              mma16816(acc[2], var, vbi.x, vbi.y);
+              mma16816(acc[2], vai, vbr.x, vbr.y);
+              mma16816(acc[3], var, vbi.z, vbi.w);
+              mma16816(acc[3], vai, vbr.z, vbr.w);
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            const long long v = (long long)__float2int_rn(acc[u][w]);
+            if (l <= 3) hi[u * 4 + w] += v << (7 * (3 - l));
+            else lo[u * 4 + w] += v << (7 * (8 - l));
+          }
+      }
+    }
+  }
+  if (!active) return;
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int i = ti * 16 + g + ((w & 2) ? 8 : 0);
+      const int j = tj * 16 + n * 8 + 2 * t + (w & 1);
+      if (i < M && j < M) {
+        const int e = ea[i] + eb[j];
+        const double re = fma((double)hi[n * 4 + w], 0x1p-35, (double)lo[n * 4 + w] * 0x1p-70);
+        const double im = fma((double)hi[8 + n * 4 + w], 0x1p-35, (double)lo[8 + n * 4 + w] * 0x1p-70);
+        out(i, j, scalbn(re, e), scalbn(im, e));
+      }
+    }
+}
+
+}  // namespace oz
+}  // namespace rg

@@ -26,6 +26,15 @@
 // factorisation (whose column fetches read W anywhere) from its update, and
 // another ends the update.
 //
+// With tensor_r (and no states kept) the sweep inverts X alone (4 M^3 +
+// O(M^2) FP64 flops) and then forms the new right-hand side B Gs1 <- X^-1
+// (B Gs1) as one complex product on the FP16 tensor cores with FP64
+// accuracy (rg_ozaki.cuh: 8 M^3 of the slice's flops leave the FP64 pipe):
+// the row exponents of X^-1 and column exponents of B Gs1 are reduced over
+// the cluster, the cluster writes both operands' digit planes to its
+// workspace, and each CTA computes 16 x 128 column groups of the product,
+// row tile by row tile, with its 8 warps.
+//
 // A diagonal pivot below sym_tau times the largest unswept entry of its
 // column flags the realization (kStatusNeedPivot, appended to flag_list);
 // launch_sweep then re-runs the flagged ones with the pivoted blocked kernel.
@@ -36,6 +45,7 @@
 #include <cooperative_groups.h>
 
 #include "rg_device.cuh"
+#include "rg_ozaki.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -49,24 +59,45 @@ constexpr int kSymMaxRowSplit = 8;
 
 // The pivot column (panel phase) and the chunk's z values (update phase)
 // share one region: they are never live at the same time.
+//
+// With tensor_r the product's staged A digits ([2][8][4][32] uint4, 32 KB)
+// overlay the start of this area (dead during the product), and two arrays
+// of 16-padded exponents follow it.
 struct LargeSymSmem {
   __host__ __device__ static size_t shared_region(int M) {
     const size_t z = (size_t)(kSymNT / 4) * 2 * kSymNB;
     return (size_t)M > z ? (size_t)M : z;
   }
-  static size_t bytes(int M) {
+  static size_t base(int M) {
     return sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
            sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
+  }
+  static constexpr size_t kStage = sizeof(uint4) * 2 * oz::kSlices * oz::kChunkTiles * 32;
+  __host__ __device__ static size_t exps_offset(int M) {
+    const size_t b = sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
+                     sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
+    return ((b > kStage ? b : kStage) + 15) & ~(size_t)15;
+  }
+  static size_t bytes(int M, bool tensor) {
+    return tensor ? exps_offset(M) + sizeof(int) * 2 * 16 * (size_t)oz::tiles(M) : base(M);
   }
 };
 
 // Workspace of one cluster, in double2 units: W, R, t (M x M each), the
 // generator states (ny x 4 uint64), the paired potential row (ny doubles)
 // and each CTA's raw pivot columns (kSymMaxCluster x NB x M).
-inline int64_t large_sym_stride(int M, int ny) {
+// With tensor_r the digit planes of both product operands and each CTA's
+// partial exponents ([kSymMaxCluster][2][16 T] ints) follow.
+__host__ __device__ inline int64_t large_sym_base_stride(int M, int ny) {
   const int64_t mm = (int64_t)M * M;
   const int64_t urow = ((int64_t)ny + 1) / 2;
   return ((3 * mm + 2 * (int64_t)ny + urow + (int64_t)kSymMaxCluster * kSymNB * M) + 15) & ~(int64_t)15;
+}
+inline int64_t large_sym_stride(int M, int ny, bool tensor) {
+  const int64_t base = large_sym_base_stride(M, ny);
+  if (!tensor) return base;
+  const int64_t ex = ((int64_t)kSymMaxCluster * 2 * 16 * oz::tiles(M) * 4 + 15) / 16;
+  return (base + 2 * oz::operand_uint4(M) + ex + 15) & ~(int64_t)15;
 }
 
 __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
@@ -98,6 +129,11 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
   const bool draw = (a.upot == nullptr);
   const bool tmat = (a.mode == kModeTmat);
   const bool refl = (a.mode == kModeRefl);
+  // the propagator product on the tensor cores (needs no per-slice states)
+  const bool gemm_on = a.tensor_r && !a.state_dump && a.inject_at == 0;
+  uint4* astage = reinterpret_cast<uint4*>(sm);  // overlays the panel arrays during the product
+  int* ea_s = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + LargeSymSmem::exps_offset(MX));
+  int* eb_s = ea_s + 16 * oz::tiles(MX);
 
   // Block argmax of the diagonal keys over the unswept indices (ties: lowest
   // index) together with a max of per-thread values `cm`; results in s_p and s_cmax.
@@ -164,6 +200,9 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
     uint64_t* gen = (uint64_t*)(ws + 3 * mm);     // [ny][4]
     double* urow_g = (double*)(gen + 4 * ny);     // [ny] paired potential row
     double2* PR = (double2*)(urow_g + ((ny + 1) & ~1)) + (int64_t)rank * NB * M;  // [NB][M] this CTA's raw pivot columns
+    uint4* adig = reinterpret_cast<uint4*>(ws + large_sym_base_stride(M, ny));  // product digit planes
+    uint4* bdig = adig + oz::operand_uint4(M);
+    int* expart = reinterpret_cast<int*>(bdig + oz::operand_uint4(M));  // [C][2][16 T] partial exponents
     if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
     const double one = a.inject_at > 0 ? 0.0 : 1.0;  // the source at slice 0, or zero until inject_at
     for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? one : 0.0, 0.0);
@@ -463,7 +502,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
         // fewest rows per thread); with T > 1 the unit's z vectors (two for
         // a pair) come through shared memory, [NT/4][2][NB] at most.
         const int P = (M + 1) / 2;
-        const int ucta = (P + M - rank + C - 1) / C;
+        const int ucta = (P + (gemm_on ? 0 : M) - rank + C - 1) / C;  // R columns only without the product
         int T = 1;
         {
           int best = ((ucta + NT - 1) / NT) * (M + 1);
@@ -534,6 +573,77 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           }
         }
         cluster.sync();
+      }
+      if (gemm_on) {
+        // 4. B Gs1 <- X^-1 (B Gs1) on the tensor cores (rg_ozaki.cuh).
+        const int T = oz::tiles(M);
+        if (n == 0) {
+          for (int64_t e = ctid; e < mm; e += CNT) {  // X^-1 I: the full symmetric inverse
+            const int i = (int)(e / M), j = (int)(e % M);
+            Rg[e] = __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i));
+          }
+        } else {
+          // a. exponents of the rows of X^-1 (symmetric: its columns too) and
+          //    of the columns of B Gs1, reduced over the cluster
+          for (int i = tid; i < 16 * T; i += NT) {
+            ea_s[i] = oz::kNoExp;
+            eb_s[i] = oz::kNoExp;
+          }
+          __syncthreads();
+          for (int64_t e = ctid; e < mm; e += CNT) {
+            const int i = (int)(e / M), j = (int)(e % M);
+            if (i <= j) {
+              const int ew = oz::fexp2(__ldcg(W + e));
+              atomicMax(ea_s + i, ew);
+              if (j != i) atomicMax(ea_s + j, ew);
+            }
+            atomicMax(eb_s + j, oz::fexp2(__ldcg(Rg + e)));
+          }
+          __syncthreads();
+          int* mine = expart + rank * 32 * T;
+          for (int i = tid; i < 16 * T; i += NT) {
+            mine[i] = ea_s[i];
+            mine[16 * T + i] = eb_s[i];
+          }
+          cluster.sync();
+          for (int i = tid; i < 16 * T; i += NT) {
+            int x = oz::kNoExp, y = oz::kNoExp;
+            for (int c = 0; c < C; ++c) {
+              x = max(x, __ldcg(expart + c * 32 * T + i));
+              y = max(y, __ldcg(expart + c * 32 * T + 16 * T + i));
+            }
+            ea_s[i] = x;
+            eb_s[i] = y;
+          }
+          __syncthreads();
+          // b. digit planes of both operands (split over the cluster)
+          oz::split_a(
+              M, [&](int i, int k) { return __ldcg(W + (i <= k ? (int64_t)i * M + k : (int64_t)k * M + i)); }, ea_s,
+              adig, ctid, CNT);
+          oz::split_b(M, [&](int k, int j) { return __ldcg(Rg + (int64_t)k * M + j); }, eb_s, bdig, ctid, CNT);
+          cluster.sync();  // every digit is written before any CTA reads them
+          // c. the product: CTA task = (row tile, group of 8 column tiles),
+          //    warp w takes column tile 8 group + w; the result overwrites
+          //    B Gs1 in place (its digits are already taken)
+          const int ngroup = (T + 7) / 8;
+          const int64_t plane = (int64_t)T * T * 32;
+          for (int task = rank; task < T * ngroup; task += C) {
+            const int ti = task / ngroup, tj = (task % ngroup) * 8 + warp;
+            auto stage = [&](int ch) {
+              __syncthreads();  // the previous chunk's digits have been used
+              const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
+              for (int e = tid; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += NT) {
+                const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
+                if (kk < nk)
+                  astage[e] = __ldcg(adig + ps * plane + ((int64_t)ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
+              }
+              __syncthreads();
+            };
+            oz::gemm_tile(M, ti, tj, tj < T, bdig, ea_s, eb_s, astage, stage,
+                          [&](int i, int j, double re, double im) { Rg[(int64_t)i * M + j] = make_double2(re, im); });
+          }
+        }
+        cluster.sync();  // the new right-hand side is complete before the next slice
       }
       if (a.state_dump && *status0 != kStatusNeedPivot) {
         // The state after this slice, natural order: Gss = W (symmetric,
@@ -697,7 +807,9 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
 
 // Same cluster-size policy as the pivoted blocked kernel (sweep_large_plan).
 int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
-  const size_t smem = LargeSymSmem::bytes(a.max_M);
+  const bool tensor = a.tensor_r && !a.state_dump && a.inject_at == 0;
+  if (tensor && a.max_M > 512) a.tensor_r = 0;  // the product's int64 fold is sized for M <= 512
+  const size_t smem = LargeSymSmem::bytes(a.max_M, a.tensor_r && tensor);
   if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes for the symmetric large-mode kernel");
   RG_CUDA(cudaFuncSetAttribute(sweep_large_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -736,13 +848,13 @@ int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_st
   if (nclusters < 1) nclusters = 1;
   a.cluster = C;
   *grid = nclusters * C;
-  *work_stride = large_sym_stride(a.max_M, a.max_ny);
+  *work_stride = large_sym_stride(a.max_M, a.max_ny, a.tensor_r && tensor);
   return RG_OK;
 }
 
 int launch_sweep_large_sym(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  const size_t smem = LargeSymSmem::bytes(a.max_M);
+  const size_t smem = LargeSymSmem::bytes(a.max_M, a.tensor_r && !a.state_dump && a.inject_at == 0);
   const int C = a.cluster > 0 ? a.cluster : 1;
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr{};

@@ -439,6 +439,14 @@ double symmetric_tau() {
   return (end && *end == '\0' && t >= 0.0) ? t : rg::kSymTau;
 }
 
+// The blocked symmetric sweep forms its propagator product on the tensor
+// cores unless RG_TENSOR_R=0 (then B Gs1 rides through the Gauss-Jordan
+// sweep in FP64 as before).
+bool tensor_r_enabled() {
+  const char* e = std::getenv("RG_TENSOR_R");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+
 // Launch arguments for items of this one waveguide (the caller sets nreal,
 // seeds or upot, outputs and the workspace).
 rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
@@ -450,6 +458,7 @@ rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
   a.max_ny = w->ny;
   a.symmetric = (w->p.boundtype == RG_BOUND_DIRICHLET && symmetric_enabled()) ? 1 : 0;
   a.sym_tau = symmetric_tau();
+  a.tensor_r = tensor_r_enabled() ? 1 : 0;
   return a;
 }
 
@@ -1182,6 +1191,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     for (int k = k0; k < k1; ++k) any_dirichlet = any_dirichlet || !descs[o_wg[k]].periodic;
     a.symmetric = (any_dirichlet && symmetric_enabled()) ? 1 : 0;
     a.sym_tau = symmetric_tau();
+    a.tensor_r = tensor_r_enabled() ? 1 : 0;
     if (maxM > rg::kMaxModesSmem) {
       // The blocked class's makespan is at least its longest item's time on
       // one CTA slot.  When that item's work times the slot count exceeds the
