@@ -320,6 +320,25 @@ int rg_probe_rate(int kind, int iters, double* tflops);
  * an FP64 product's level).  For tests and measurements. */
 int rg_ozaki_zgemm(int M, const double* a, const double* b, double* c);
 
+/* No counterpart in the reference (the adjoint's per-slice products): for
+ * k < nbatch,
+ *     C_k = alpha * op(A_k) diag(s) op(B_k) + beta * D_k
+ * with M x M complex matrices (1 <= M <= 512) on the device, through the same
+ * tensor-core path as rg_ozaki_zgemm.  Operand X of item k is the matrix at
+ * x + (k % mod_x) * stride_x (complex elements; mod_x <= 0 means nbatch), so
+ * an operand can be shared by several items; op 0 = X, 1 = X^T, 2 = X^H;
+ * rowscale_b (M complex, may be NULL) is diag(s); D may be NULL when beta is
+ * 0.  colmajor != 0: column-major matrices, else row-major (C order).  C may
+ * alias A, B or D.  workspace (device, 16-byte aligned) holds at least
+ * rg_zgemm_workspace_bytes(M, nbatch) bytes; the call allocates nothing and
+ * enqueues three kernels on `stream` (taken literally), without
+ * synchronising. */
+int64_t rg_zgemm_workspace_bytes(int M, int nbatch);
+int rg_zgemm_batched(int M, int nbatch, const double* a, int64_t stride_a, int mod_a, int op_a, const double* b,
+                     int64_t stride_b, int mod_b, int op_b, const double* rowscale_b, double alpha_re,
+                     double alpha_im, const double* d, int64_t stride_d, int mod_d, double beta, double* c,
+                     int64_t stride_c, int colmajor, void* workspace, int64_t workspace_bytes, void* stream);
+
 /* histogram (src/base_utils.f90:491-516) with the reference's exact edge
  * semantics, computed on the GPU: samples[n] and bins[nbins+1] are host
  * arrays; histo[nbins] and *missing receive counts as doubles. */

@@ -31,7 +31,7 @@ EXPORTS = (
     "rg_tprofile_batch", "rg_compute_tprofile", "rg_compute_itx_profile", "rg_compute_tprofile_group",
     "rg_compute_deposition", "rg_deposition_batch", "rg_compute_wavefunction", "rg_diagonalize_ahca",
     "rg_sweep_states", "rg_compute_refl_trans_v2", "rg_probe_rate",
-    "rg_ozaki_zgemm",
+    "rg_ozaki_zgemm", "rg_zgemm_workspace_bytes", "rg_zgemm_batched",
 )
 PROFILE_KINDS = {"tprofile": 0, "itx": 1, "group": 2}
 KERNELS = {0: "pivoted", 1: "symmetric", 2: "blocked", 3: "blocked_symmetric"}
@@ -103,6 +103,11 @@ def lib() -> C.CDLL:
     L.rg_compute_refl_trans_v2.argtypes = [vp, C.c_int, vp, vp]
     L.rg_probe_rate.argtypes = [C.c_int, C.c_int, dp]
     L.rg_ozaki_zgemm.argtypes = [C.c_int, vp, vp, vp]
+    L.rg_zgemm_workspace_bytes.argtypes = [C.c_int, C.c_int]
+    L.rg_zgemm_workspace_bytes.restype = C.c_int64
+    L.rg_zgemm_batched.argtypes = ([C.c_int, C.c_int, vp, i64, C.c_int, C.c_int, vp, i64, C.c_int, C.c_int, vp,
+                                    C.c_double, C.c_double, vp, i64, C.c_int, C.c_double, vp, i64, C.c_int, vp, i64,
+                                    vp])
     _LIB = L
     return L
 

@@ -37,8 +37,10 @@ mode through the recursion, with Gamma = dL/dt*:
 
 In both, dL/dU_n = -2 sum Re(Xbar_n[a][c]) chi_a chi_c (rg_adjoint_grad_rows).
 The per-slice complex products are batched over realizations and losses
-(cuBLAS through torch); the sweeps and the gradient rows are this library's
-kernels.
+and run on the tensor cores with FP64 accuracy (rg_zgemm_batched, the
+digit-split products of the sweep's propagator); the sweeps and the
+gradient rows are this library's kernels too.  Only elementwise torch
+operations remain around them.
 """
 from __future__ import annotations
 
@@ -111,12 +113,56 @@ class TransmissionLosses(torch.autograd.Function):
         B, dev = U.shape[0], U.device
         g1 = torch.zeros(B, dtype=torch.float64, device=dev) if g1 is None else g1
         g2 = torch.zeros(B, dtype=torch.float64, device=dev) if g2 is None else g2
-        Gamma = g1[:, None, None] * t + g2[:, None, None] * 2.0 * (t @ (t.conj().transpose(1, 2) @ t))
+        Gamma = g1[:, None, None] * t + g2[:, None, None] * _gamma2(t)
         if ctx.method == "green":
             dU = _green_backward(ctx.wg, U, lambda b0, b1, tc: Gamma[None, b0:b1])
         else:
             dU = _reverse_sweep(ctx.wg, U, ckpt, ctx.K, Gamma[None])
         return dU[0], None, None, None
+
+
+class _ZGemm:
+    """Batched M x M complex products C_k = alpha op(A_k) diag(s) op(B_k) + beta D_k
+    on the tensor cores (rg_zgemm_batched), on row-major complex128 tensors
+    whose last two dimensions are (M, M).  An operand with fewer items than
+    the batch is shared cyclically (item k uses matrix k % len)."""
+
+    def __init__(self, M: int, nmax: int, dev):
+        self.M, self.nmax = M, nmax
+        nb = int(lib().rg_zgemm_workspace_bytes(M, nmax))
+        self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+        self.stream = _vp(torch.cuda.current_stream().cuda_stream)
+
+    def _op(self, X: torch.Tensor):
+        X = X if X.dim() == 3 else X.reshape(-1, self.M, self.M)
+        assert X.dtype == torch.complex128 and X.stride(-1) == 1 and X.stride(-2) == self.M
+        return _vp(X.data_ptr()), X.stride(0) if X.shape[0] > 1 else 0, X.shape[0]
+
+    def __call__(self, n, A, B, C, opA=0, opB=0, rowscale=None, alpha=1.0, D=None, beta=0.0):
+        assert n <= self.nmax
+        pa, sa, ma = self._op(A)
+        pb, sb, mb = self._op(B)
+        pc, sc, _ = self._op(C)
+        pd, sd, md = self._op(D) if D is not None else (None, 0, 1)
+        alpha = complex(alpha)
+        _check(lib().rg_zgemm_batched(self.M, n, pa, sa, ma, opA, pb, sb, mb, opB, _ptr(rowscale), alpha.real,
+                                      alpha.imag, pd, sd, md, beta, pc, sc, 0, _vp(self.ws.data_ptr()),
+                                      self.ws.numel(), self.stream))
+        return C
+
+
+def _bmm(A: torch.Tensor, B: torch.Tensor, opA: int = 0, opB: int = 0) -> torch.Tensor:
+    """op(A) op(B) for batches of square matrices on the tensor cores
+    (rg_zgemm_batched); rectangular ones (ragged filter windows) through torch."""
+    M = A.shape[-1]
+    if A.shape[-2] == M and B.shape[-2:] == (M, M) and M <= 512 and A.is_cuda:
+        A, B = A.contiguous(), B.contiguous()
+        n = max(A.reshape(-1, M, M).shape[0], B.reshape(-1, M, M).shape[0])
+        C = torch.empty(n, M, M, dtype=torch.complex128, device=A.device)
+        _ZGemm(M, n, A.device)(n, A, B, C, opA=opA, opB=opB)
+        return C.reshape(B.shape if B.dim() >= A.dim() else A.shape)
+    f = {0: lambda x: x, 1: lambda x: x.transpose(-1, -2), 2: lambda x: x.conj().transpose(-1, -2)}
+    return f[opA](A) @ f[opB](B)
 
 
 def _check_input(U: torch.Tensor, wg: Waveguide) -> torch.Tensor:
@@ -129,8 +175,13 @@ def _check_input(U: torch.Tensor, wg: Waveguide) -> torch.Tensor:
 
 
 def _losses(t: torch.Tensor):
-    A = t.conj().transpose(1, 2) @ t
+    A = _bmm(t, t, opA=2)  # t^H t
     return (t.abs() ** 2).sum((1, 2)), (A.abs() ** 2).sum((1, 2))
+
+
+def _gamma2(t: torch.Tensor) -> torch.Tensor:
+    """dL2/dt* = 2 t (t^H t)."""
+    return 2.0 * _bmm(t, _bmm(t, t, opA=2))
 
 
 def _states_bytes(wg: Waveguide) -> int:
@@ -203,17 +254,24 @@ def _green_backward(wg: Waveguide, U: torch.Tensor, gamma_of):
         G[:, :, r0:r0 + Gamma.shape[2], c0:c0 + Gamma.shape[3]] = Gamma
         P = sq[:, None] * G.conj().transpose(-1, -2) * sq[None, :]  # S Gamma~^H S
         dU = torch.zeros(S, b1 - b0, nxdiso, ny, dtype=U.dtype, device=dev)
+        nb = b1 - b0
+        zg = _ZGemm(M, S * nb, dev)
+        P = P.reshape(S * nb, M, M).contiguous()
         X1 = states[:, nx - 1, 1].clone()  # G(N,1) = Z_N
         XN = states[:, nx - 1, 0].clone()  # G(N,N) = S_N
+        Y = torch.empty(S * nb, M, M, dtype=torch.complex128, device=dev)
+        K = torch.empty_like(Y)
+        bflat = bvec.reshape(M).contiguous()
         for n in reversed(range(nx)):
             if n < nx - 1:
-                Sn = states[:, n, 0]
-                X1 = states[:, n, 1] - Sn @ (bvec * X1)
-                XN = -(Sn @ (bvec * XN))
+                Sn, Zn = states[:, n, 0], states[:, n, 1]
+                zg(nb, Sn, X1, X1, rowscale=bflat, alpha=-1.0, D=Zn, beta=1.0)  # X1 = Z_n - S_n B X1
+                zg(nb, Sn, XN, XN, rowscale=bflat, alpha=-1.0)  # XN = -S_n B XN
             idd = n - nxfree
             if 0 <= idd < nxdiso:
-                K = ((-2j) * ((X1 @ P) @ XN.transpose(-1, -2))).contiguous()
-                _check(lib().rg_adjoint_grad_rows(wg._h, _ptr(K), S * (b1 - b0), _vp(dU.data_ptr() + 8 * idd * ny),
+                zg(S * nb, X1, P, Y)  # Y = G(n,1) P, G(n,1) shared by the S losses
+                zg(S * nb, Y, XN, K, opB=1, alpha=-2j)  # K = -2i Y G(n,N)^T
+                _check(lib().rg_adjoint_grad_rows(wg._h, _ptr(K), S * nb, _vp(dU.data_ptr() + 8 * idd * ny),
                                                   nxdiso * ny, stream))
         out[:, b0:b1] = dU
         del states
@@ -260,21 +318,27 @@ def _reverse_sweep(wg: Waveguide, U: torch.Tensor, ckpt: torch.Tensor, K: int, G
     Gssbar = torch.zeros_like(Gs1bar)
     dU = torch.zeros((S,) + tuple(U.shape), dtype=U.dtype, device=dev)
     nxdiso, ny, nxfree = wg.nxdiso, wg.ny, wg.nxfree
+    zg = _ZGemm(M, S * B, dev)
+    Gs1bar_prev = torch.empty_like(Gs1bar)
+    Xbar = torch.empty_like(Gs1bar)
+    tmp = torch.empty_like(Gs1bar)
     for s in reversed(range(len(sw.segs))):
         b, e = sw.segs[s]
         sin = ckpt[s - 1] if s > 0 else None
         dump = torch.empty(B, e - b, 2, M, M, dtype=torch.complex128, device=dev)
         sw.run(b, e, sin, dump=dump)
         for n in reversed(range(b, e)):
-            Gss = dump[:, n - b, 0]
-            GssH = Gss.conj().transpose(1, 2)
+            Gss = dump[:, n - b, 0]  # shared by the S chains
             if n > 0:
                 Gs1_prev = dump[:, n - 1 - b, 1] if n - 1 >= b else sin[:, 1]
-                Gssbar = Gssbar - Gs1bar @ (bvec[:, None] * Gs1_prev).conj().transpose(1, 2)
-                Gs1bar_prev = -(bc[:, None] * (GssH @ Gs1bar))
+                bG = (bvec[:, None] * Gs1_prev).contiguous()
+                zg(S * B, Gs1bar, bG, Gssbar, opB=2, alpha=-1.0, D=Gssbar, beta=1.0)  # -= Gs1bar (B Gs1)^H
+                zg(S * B, Gss, Gs1bar, Gs1bar_prev, opA=2, alpha=-1.0)
+                Gs1bar_prev *= bc[:, None]  # -conj(B) Gss^H Gs1bar
             else:
                 Gssbar = Gssbar + Gs1bar
-            Xbar = (-(GssH @ Gssbar) @ GssH).contiguous()
+            zg(S * B, Gss, Gssbar, tmp, opA=2)
+            zg(S * B, tmp, Gss, Xbar, opB=2, alpha=-1.0)  # -Gss^H Gssbar Gss^H
             idd = n - nxfree
             if 0 <= idd < nxdiso:
                 # rows of all S*B realizations: dU is (S, B, nxdiso, ny)
@@ -282,7 +346,7 @@ def _reverse_sweep(wg: Waveguide, U: torch.Tensor, ckpt: torch.Tensor, K: int, G
                                                   nxdiso * ny, _vp(sw.stream.cuda_stream)))
             if n > 0:
                 Gssbar = -(bc[:, None] * Xbar * bc[None, :])
-                Gs1bar = Gs1bar_prev
+                Gs1bar, Gs1bar_prev = Gs1bar_prev, Gs1bar
     sw.check_status()
     return dU
 
@@ -306,12 +370,12 @@ def transmission_losses_and_grads(U: torch.Tensor, wg: Waveguide, K: int = 0, me
 
         def gamma_of(b0, b1, t):
             ts[b0] = t
-            return torch.stack([t, 2.0 * (t @ (t.conj().transpose(1, 2) @ t))])
+            return torch.stack([t, _gamma2(t)])
 
         dU = _green_backward(wg, U, gamma_of)
         L1, L2 = _losses(torch.cat([ts[k] for k in sorted(ts)]))
         return L1, L2, dU[0], dU[1]
     L1, L2, Ud, t, ckpt, K = _forward(U, wg, K)
-    Gamma = torch.stack([t, 2.0 * (t @ (t.conj().transpose(1, 2) @ t))])
+    Gamma = torch.stack([t, _gamma2(t)])
     dU = _reverse_sweep(wg, Ud, ckpt, K, Gamma)
     return L1, L2, dU[0], dU[1]

@@ -128,9 +128,8 @@ struct SweepArgs {
   int inject_at;
   // 1: the blocked symmetric kernel forms the propagator product Gss (B Gs1)
   // on the tensor cores (rg_ozaki.cuh) after inverting X on its own, instead
-  // of carrying B Gs1 through the Gauss-Jordan sweep; used when no states
-  // are kept (state_dump == nullptr, inject_at == 0).  Set from RG_TENSOR_R
-  // (default on).
+  // of carrying B Gs1 through the Gauss-Jordan sweep (up to 512 modes).
+  // Set from RG_TENSOR_R (default on).
   int tensor_r;
 };
 
@@ -220,6 +219,7 @@ struct GreenView {
   const cplx* sqmu_r;    // host [nmu] sqrt(real(mu))
   int symmetric;         // the symmetric sweep is enabled for this guide (Dirichlet)
   double sym_tau;        // its pivot threshold
+  int tensor_r;          // SweepArgs::tensor_r for this guide
 };
 int green_view(const rg_waveguide* w, GreenView* out);
 

@@ -26,7 +26,7 @@
 // factorisation (whose column fetches read W anywhere) from its update, and
 // another ends the update.
 //
-// With tensor_r (and no states kept) the sweep inverts X alone (4 M^3 +
+// With tensor_r the sweep inverts X alone (4 M^3 +
 // O(M^2) FP64 flops) and then forms the new right-hand side B Gs1 <- X^-1
 // (B Gs1) as one complex product on the FP16 tensor cores with FP64
 // accuracy (rg_ozaki.cuh: 8 M^3 of the slice's flops leave the FP64 pipe):
@@ -129,8 +129,8 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
   const bool draw = (a.upot == nullptr);
   const bool tmat = (a.mode == kModeTmat);
   const bool refl = (a.mode == kModeRefl);
-  // the propagator product on the tensor cores (needs no per-slice states)
-  const bool gemm_on = a.tensor_r && !a.state_dump && a.inject_at == 0;
+  // the propagator product on the tensor cores
+  const bool gemm_on = a.tensor_r != 0;
   uint4* astage = reinterpret_cast<uint4*>(sm);  // overlays the panel arrays during the product
   int* ea_s = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + LargeSymSmem::exps_offset(MX));
   int* eb_s = ea_s + 16 * oz::tiles(MX);
@@ -577,10 +577,15 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
       if (gemm_on) {
         // 4. B Gs1 <- X^-1 (B Gs1) on the tensor cores (rg_ozaki.cuh).
         const int T = oz::tiles(M);
-        if (n == 0) {
-          for (int64_t e = ctid; e < mm; e += CNT) {  // X^-1 I: the full symmetric inverse
+        if (n < a.inject_at) {
+          // before the source slice the right-hand side is zero and stays zero
+        } else if (n == a.inject_at) {
+          // X^-1 (+-I) at the source slice: the full symmetric inverse itself
+          // (+I at slice 0, -I at a later source slice)
+          const double sg = n == 0 ? 1.0 : -1.0;
+          for (int64_t e = ctid; e < mm; e += CNT) {
             const int i = (int)(e / M), j = (int)(e % M);
-            Rg[e] = __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i));
+            Rg[e] = cscale(sg, __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i)));
           }
         } else {
           // a. exponents of the rows of X^-1 (symmetric: its columns too) and
@@ -807,9 +812,9 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
 
 // Same cluster-size policy as the pivoted blocked kernel (sweep_large_plan).
 int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_stride) {
-  const bool tensor = a.tensor_r && !a.state_dump && a.inject_at == 0;
-  if (tensor && a.max_M > 512) a.tensor_r = 0;  // the product's int64 fold is sized for M <= 512
-  const size_t smem = LargeSymSmem::bytes(a.max_M, a.tensor_r && tensor);
+  if (a.max_M > 512) a.tensor_r = 0;  // the product's int64 fold is sized for M <= 512
+  const bool tensor = a.tensor_r != 0;
+  const size_t smem = LargeSymSmem::bytes(a.max_M, tensor);
   if (smem > 227 * 1024) return fail(RG_ERR_INVALID_ARG, "too many modes for the symmetric large-mode kernel");
   RG_CUDA(cudaFuncSetAttribute(sweep_large_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -848,13 +853,13 @@ int sweep_large_sym_plan(SweepArgs& a, int sm_count, int* grid, int64_t* work_st
   if (nclusters < 1) nclusters = 1;
   a.cluster = C;
   *grid = nclusters * C;
-  *work_stride = large_sym_stride(a.max_M, a.max_ny, a.tensor_r && tensor);
+  *work_stride = large_sym_stride(a.max_M, a.max_ny, tensor);
   return RG_OK;
 }
 
 int launch_sweep_large_sym(const SweepArgs& a, cudaStream_t stream, int grid) {
   if (a.nreal <= 0) return RG_OK;
-  const size_t smem = LargeSymSmem::bytes(a.max_M, a.tensor_r && !a.state_dump && a.inject_at == 0);
+  const size_t smem = LargeSymSmem::bytes(a.max_M, a.tensor_r != 0);
   const int C = a.cluster > 0 ? a.cluster : 1;
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr{};

@@ -810,6 +810,7 @@ int green_view(const rg_waveguide* w, GreenView* out) {
   const SweepArgs a = make_args(w, kModeEig);
   out->symmetric = a.symmetric;
   out->sym_tau = a.sym_tau;
+  out->tensor_r = a.tensor_r;
   return RG_OK;
 }
 
