@@ -289,9 +289,9 @@ int rg_last_batch_info(rg_waveguide* wg, rg_batch_info* info);
 
 /* No counterpart in the reference.  One seed's transmission eigenvalues, as
  * rg_compute_tdistrib computes them, for callers that cannot allocate device
- * memory when they need the result: code running during CUDA stream capture,
- * hosts whose device memory is handed to their own pool, and loops that must
- * not take cudaMalloc's implicit synchronisation.  The call allocates nothing:
+ * memory when they need the result: hosts whose device memory is handed to
+ * their own pool allocator, and loops that must not take cudaMalloc's
+ * implicit synchronisation.  The call allocates nothing:
  * create the handle with rg_init at set-up, then call this with device
  * buffers d_teigvals[neigv] and d_status[1]; work is enqueued on `stream`
  * (NULL: the handle's stream) and the call returns without synchronising.
@@ -300,7 +300,9 @@ int rg_last_batch_info(rg_waveguide* wg, rg_batch_info* info);
  * the elimination matrices, about 64*nmu^2 bytes, share the array too);
  * larger guides get RG_ERR_INVALID_ARG.  The handle's device must be current; the first
  * call on each device looks the array up (make it before any stream capture).
- * Calls that overlap on the GPU race on the shared array. */
+ * Calls that overlap on the GPU race on the shared array.  iseed must be >= 1.
+ * The array's address is kept per device index for the life of the process:
+ * do not call this after the device was reset (cudaDeviceReset). */
 int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_teigvals, int32_t* d_status, void* stream);
 
 /* No counterpart in the reference: throughput of one arithmetic pipe of the

@@ -2,10 +2,9 @@
 // realization with no device allocation in the call.
 //
 // Why it exists: some callers cannot call cudaMalloc at the point where they
-// need a result -- code running while a CUDA stream is being captured (where
-// allocation calls are not permitted), host applications that hand all device
-// memory to their own pool allocator, and steady-state loops that must not
-// take cudaMalloc's implicit device synchronisation.  They create the
+// need a result -- host applications that hand all device memory to their
+// own pool allocator, and steady-state loops that must not take cudaMalloc's
+// implicit device synchronisation.  They create the
 // waveguide handle once at set-up (rg_init allocates its tables there) and
 // then call this entry point, which only launches kernels on memory that
 // already exists.
@@ -66,6 +65,8 @@ extern "C" int rg_tdistrib_seed_noalloc(rg_waveguide* wg, int iseed, double* d_t
                                         void* stream) {
   if (!wg || !d_teigvals || !d_status)
     return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_seed_noalloc: NULL argument");
+  if (iseed < 1)  // the same seeds as rg_compute_tdistrib accepts
+    return rg::fail(RG_ERR_INVALID_ARG, "rg_tdistrib_seed_noalloc: iseed must be >= 1");
   rg::NoAllocView v{};
   int rc = rg::noalloc_view(wg, &v);
   if (rc) return rc;

@@ -421,7 +421,10 @@ void create_directory(const std::string& dir) {
 namespace {
 
 void write_preamble(std::FILE* fp, const recurgreen::Waveguide& w, long nseed, long nbins, long nthreads,
-                    double tsec) {
+                    double tsec, long seed0 = 1) {
+  // a run that starts at seed0 != 1 names its seed range, so files of
+  // disjoint ranges stay apart
+  if (seed0 != 1) std::fprintf(fp, "%%%% Seeds %ld..%ld\n", seed0, seed0 + nseed - 1);
   std::fprintf(fp, "%%%% Computed on %s by %s\n", timestamp().c_str(), kProgram);
   w.print_parameters(fp, "%%");
   const double speed = nseed / tsec;
@@ -469,6 +472,8 @@ void task_tdistrib(const std::string& text, const std::string& root) {
   if (nseed < 0) throw Stop("Invalid number of seeds, received " + fmt_int(nseed) + " expected >=0, aborting...");
   if (nbins < 1) throw Stop("Invalid number of bins, received " + fmt_int(nbins) + " expected >0, aborting...");
   if (seed0 < 1) throw Stop("Invalid first seed, received seed0=" + fmt_int(seed0) + ", expected >0, aborting...");
+  if (seed0 + nseed - 1 > 2147483647L)
+    throw Stop("Invalid seed range, seed0+nseed-1=" + fmt_int(seed0 + nseed - 1) + " exceeds 2147483647, aborting...");
 
   // The seed loop (src/main.f90:134-179) as one batched GPU launch.
   std::vector<int32_t> seeds(nseed);
@@ -494,7 +499,7 @@ void task_tdistrib(const std::string& text, const std::string& root) {
   const std::string fname = unique_filename(dir + "result_", ".distrib.csv");
   std::FILE* fp = std::fopen(fname.c_str(), "w");
   if (!fp) throw Stop("Cannot open file: " + fname);
-  write_preamble(fp, w, nseed, nbins, nthreads, tsec);
+  write_preamble(fp, w, nseed, nbins, nthreads, tsec, seed0);
   std::fprintf(fp, "tm, rho\n");
   write_rows(fp, d);
   std::fclose(fp);
@@ -503,7 +508,7 @@ void task_tdistrib(const std::string& text, const std::string& root) {
     const std::string ename = unique_filename(dir + "result_", ".eigvals.csv");
     std::FILE* fe = std::fopen(ename.c_str(), "w");
     if (!fe) throw Stop("Cannot open file: " + ename);
-    write_preamble(fe, w, nseed, nbins, nthreads, tsec);
+    write_preamble(fe, w, nseed, nbins, nthreads, tsec, seed0);
     std::fprintf(fe, "%%%% Transmission eigenvalues (%zu values)\n", tallvals.size());
     for (double v : tallvals) std::fprintf(fe, "%s\n", format_g0(v).c_str());
     std::fclose(fe);

@@ -192,11 +192,15 @@ def unique_filename(base: str, ext: str) -> str:
     return f"{base}{i}{ext}"
 
 
-def _preamble(w: Waveguide, nseed: int, nbins: int, nthreads: int, tsec: float, prefix: str = "%%") -> list[str]:
+def _preamble(w: Waveguide, nseed: int, nbins: int, nthreads: int, tsec: float, prefix: str = "%%",
+              seed0: int = 1) -> list[str]:
+    """The reference's header lines; a run that starts at seed0 != 1 adds one
+    line naming its seed range, so files of disjoint ranges stay apart."""
     p = w.get_parameters()
     now = datetime.datetime.now().astimezone()
     speed = nseed / tsec if tsec > 0 else float("inf")
-    return [
+    extra = [f"{prefix} Seeds {seed0}..{seed0 + nseed - 1}"] if seed0 != 1 else []
+    return extra + [
         f"{prefix} Computed on {now:%Y-%m-%d at %H:%M:%S %z} by {PROGRAM}",
         f"{prefix} Waveguide 2D with boundtype='{p['boundtype']}', W/lambda={fortran_f(p['wol'])}, "
         f"exfac={fortran_f(p['exfac'])}, Nmode={w.nmu}, Nprop={w.nprop}",
@@ -255,10 +259,12 @@ def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
     seeds at seed0: runs on separate machines over disjoint ranges give
     eigenvalue files that together are the run over their union."""
     td = settings["tdistrib"]
-    w = _waveguide_from(settings["waveguide"])
     nseed, nbins, seed0 = int(td["nseed"]), int(td["nbins"]), int(td.get("seed0", 1))
     if seed0 < 1:
         raise ValueError(f"Invalid first seed, received seed0={seed0}, expected >0, aborting...")
+    if seed0 + nseed - 1 > 2 ** 31 - 1:
+        raise ValueError(f"Invalid seed range, seed0+nseed-1={seed0 + nseed - 1} exceeds 2147483647, aborting...")
+    w = _waveguide_from(settings["waveguide"])
     if group is not None:
         return _task_tdistrib_replicas(w, td, nseed, nbins, outdir, group, seed0)
     t0 = time.perf_counter()
@@ -267,7 +273,7 @@ def task_tdistrib(settings: dict, outdir: str = "out", group=None) -> dict:
     rho, missing = prepare_distrib(tallvals, nbins)
     ddir = os.path.join(generate_directory(w, outdir), "distrib")
     os.makedirs(ddir, exist_ok=True)
-    pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec)
+    pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec, seed0=seed0)
     dpath = unique_filename(os.path.join(ddir, "result_"), ".distrib.csv")
     save_distrib(dpath, rho, pre)
     res = {"distrib": dpath, "tallvals": tallvals, "rho": rho, "missing": missing, "time": tsec}
@@ -298,7 +304,7 @@ def _task_tdistrib_replicas(w: Waveguide, td: dict, nseed: int, nbins: int, outd
     if rank == 0:
         ddir = os.path.join(generate_directory(w, outdir), "distrib")
         os.makedirs(ddir, exist_ok=True)
-        pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec)
+        pre = _preamble(w, nseed, nbins, int(td.get("nthreads", 1)), tsec, seed0=seed0)
         res["distrib"] = unique_filename(os.path.join(ddir, "result_"), ".distrib.csv")
         save_distrib(res["distrib"], rho, pre)
         if tallvals is not None:

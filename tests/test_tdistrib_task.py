@@ -126,3 +126,13 @@ def test_task_tdistrib_replica_path_matches(tmp_path):
     np.testing.assert_array_equal(rep["rho"], plain["rho"])
     np.testing.assert_array_equal(rep["tallvals"], plain["tallvals"])
     assert open(rep["distrib"]).read().splitlines()[5:] == open(plain["distrib"]).read().splitlines()[5:]
+
+
+def test_seed_range_checked_before_any_device_work():
+    """seed0 < 1 and seed ranges past the int32 seeds of the C ABI are rejected
+    (no GPU needed: the check comes before the waveguide is built)."""
+    s = T.read_namelists(NML)
+    for seed0, nseed in ((0, 10), (2 ** 31 - 5, 10)):
+        s["tdistrib"]["seed0"], s["tdistrib"]["nseed"] = seed0, nseed
+        with pytest.raises(ValueError):
+            T.task_tdistrib(s, "/nonexistent")

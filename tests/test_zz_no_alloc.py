@@ -1,6 +1,6 @@
 """rg_tdistrib_seed_noalloc: the entry point for callers that cannot allocate
-device memory at call time (stream capture, pool-managed device memory,
-latency-critical loops).  It draws the potential into the library's fixed
+device memory at call time (pool-managed device memory, latency-critical
+loops).  It draws the potential into the library's fixed
 16 MiB device array instead of allocated scratch; its results must equal the
 allocating entry point rg_compute_tdistrib's, on consecutive calls that
 reuse the shared array.  Collected last on purpose (file name)."""
@@ -61,3 +61,9 @@ def test_noalloc_rejects_guides_beyond_capacity():
     rc = L.rg_tdistrib_seed_noalloc(g._h, 1, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(st.data_ptr()), None)
     assert rc == rg.RG_ERR_INVALID_ARG
     assert b"capacity" in L.rg_last_error()
+    # seeds below 1 are rejected, as by rg_compute_tdistrib
+    small = rg.Waveguide("dirichlet", nxdiso=20, nxfree=0, wol=5.25, exfac=1.0, dscat=5.0, ny=64)
+    for bad in (0, -3):
+        rc = L.rg_tdistrib_seed_noalloc(small._h, bad, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(st.data_ptr()),
+                                        None)
+        assert rc == rg.RG_ERR_INVALID_ARG and b"iseed" in L.rg_last_error()
