@@ -73,6 +73,28 @@ SPECS = {
 }
 
 
+def uneven_items(n: int = 2048) -> list[tuple[dict, int]]:
+    """The batched-uneven workload: guide k (seed k + 1) has N drawn from
+    {32, 48, 64, 96, 128, 192, 256} (kW/pi = N + 0.5, M = N, ny = 4N),
+    Nx from [500, 5000], L/l_s from [1, 20], and absorption
+    eps = 0.01 k^2 (dabso = 0.02 pi W/lambda) with probability 1/2, all from
+    numpy default_rng(0)."""
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    Ns = [32, 48, 64, 96, 128, 192, 256]
+    out = []
+    for k in range(n):
+        N = int(rng.choice(Ns))
+        nx = int(rng.integers(500, 5001))
+        ds = float(rng.uniform(1, 20))
+        wol = (N + 0.5) / 2
+        dabso = 0.02 * math.pi * wol if rng.random() < 0.5 else 0.0
+        out.append((dict(boundtype="dirichlet", nxdiso=nx, nxfree=0, wol=wol, exfac=1.0, aratio=1.0, dscat=ds,
+                         dabso=dabso, ny=4 * N), k + 1))
+    return out
+
+
 def flops_per_realization(M: int, nx: int) -> float:
     """Algorithmic FP64 flops of the reference's sweep (src/waveguide.f90:426-440):
     16 M^3 per slice (complex inverse 8 M^3 + complex product 8 M^3) for
@@ -390,9 +412,33 @@ def run_workload(args) -> None:
             if rc:
                 raise rg.RecurGreenError(rc, L.rg_last_error().decode())
             rates[name] = v.value
+        # the tensor-core complex product (rg_zgemm_batched) at the sweep's
+        # sizes: 152 independent M x M products per call, FP16 flops counted as
+        # 43 digit pairs x 4 real products x 2 M^3
+        from recurgreen_gb300.adjoint import _ZGemm
+        zrates = {}
+        for M in (128, 256, 512):
+            nb = 152
+            A = torch.randn(nb, M, M, dtype=torch.complex128, device="cuda")
+            B = torch.randn(nb, M, M, dtype=torch.complex128, device="cuda")
+            C = torch.empty_like(A)
+            zg = _ZGemm(M, nb, A.device)
+            zg(nb, A, B, C)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                zg(nb, A, B, C)
+            e1.record()
+            e1.synchronize()
+            sec = e0.elapsed_time(e1) / 3e3
+            zrates[f"M{M}"] = {"ms_per_call": 1e3 * sec, "fp16_tflops": 43 * 4 * 2 * M ** 3 * nb / sec / 1e12,
+                               "fp64_equivalent_tflops": 8 * M ** 3 * nb / sec / 1e12}
+            del A, B, C, zg
         out["clocks"] = clk.stop()
         out["tflops"] = rates
         out["tflops"]["cublas_dgemm_8192"] = peak
+        out["zgemm_batched"] = zrates
         out.pop("fp64_peak_tflops")
     elif args.workload == "large":
         kw = dict(BASE, wol=256.25, nxdiso=args.nx or 10000, dscat=20.0, ny=2048)
@@ -422,22 +468,15 @@ def run_workload(args) -> None:
             out["per_realization_sample"] = f"{args.per_sample} seeds, one rg_compute_tdistrib call each, {pdt:.1f} s"
             out["batched_over_per_realization"] = out["batched_realizations_per_s"] / pr
     elif args.workload == "uneven":
-        rng = np.random.default_rng(0)
         Ns = [32, 48, 64, 96, 128, 192, 256]
         n = args.batch or 2048
         guides, items, fl = {}, [], 0.0
         t0 = time.perf_counter()
-        for k in range(n):
-            N = int(rng.choice(Ns))
-            nx = int(rng.integers(500, 5001))
-            ds = float(rng.uniform(1, 20))
-            wol = (N + 0.5) / 2
-            dabso = 0.02 * math.pi * wol if rng.random() < 0.5 else 0.0
-            g = rg.Waveguide("dirichlet", nxdiso=nx, nxfree=0, wol=wol, exfac=1.0, aratio=1.0, dscat=ds,
-                             dabso=dabso, ny=4 * N)
+        for k, (kw, seed) in enumerate(uneven_items(n)):
+            g = rg.Waveguide(**kw)
             guides[k] = g
-            items.append((g, k + 1))
-            fl += flops_per_realization(g.nmu, nx)
+            items.append((g, seed))
+            fl += flops_per_realization(g.nmu, kw["nxdiso"])
         t_init = time.perf_counter() - t0
         clk.start()
         dt, (res, st) = _sync_time(torch, lambda: rg.tdistrib_multi(items, return_status=True))
