@@ -121,6 +121,10 @@ struct SweepArgs {
   const int* count_ptr;       // device-side queue length; nullptr: nreal
   int force_cluster;          // > 0: cluster size for the blocked kernels instead of the heuristic
                               // (autotuner, multi calls with long items)
+  int force_rowsplit;         // > 0: threads per update unit of the blocked symmetric kernel (1, 4
+                              // or 8) instead of its fewest-rows-per-thread rule (autotuner)
+  int force_per_sm;           // > 0: at most this many CTAs per SM for the shared-memory kernels
+                              // (autotuner); 0: the occupancy limit
   // Source slice of the Green-function column (pivoted blocked kernel, fresh
   // start): Gs1 after slice n is Z_n of solve_block_tridiag for the identity
   // source at slice inject_at (src/base_utils.f90:318-324), zero before it.

@@ -449,6 +449,7 @@ int plan_t(SweepArgs& a, int sm_count, int* grid, int64_t* stride) {
   int per_sm = 0;
   RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<MCAP, NT, MINB>, NT, smem));
   if (per_sm < 1) return fail(RG_ERR_INVALID_ARG, "sweep kernel does not fit on an SM (ny too large?)");
+  if (a.force_per_sm > 0 && a.force_per_sm < per_sm) per_sm = a.force_per_sm;
   int g = per_sm * sm_count;
   if (g > a.nreal) g = a.nreal;
   *grid = g < 1 ? 1 : g;

@@ -504,7 +504,9 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
         const int P = (M + 1) / 2;
         const int ucta = (P + (gemm_on ? 0 : M) - rank + C - 1) / C;  // R columns only without the product
         int T = 1;
-        {
+        if (a.force_rowsplit == 1 || a.force_rowsplit == 4 || a.force_rowsplit == 8) {
+          T = a.force_rowsplit;  // the autotuner's choice (the same arithmetic per element)
+        } else {
           int best = ((ucta + NT - 1) / NT) * (M + 1);
           for (int t = 4; t <= kSymMaxRowSplit; t *= 2) {
             const int rows = ((ucta + NT / t - 1) / (NT / t)) * ((M + 1 + t - 1) / t);

@@ -176,7 +176,7 @@ void jump_polynomial(uint64_t distance, uint64_t out[4]) {
 // The waveguide handle.
 // ---------------------------------------------------------------------------
 // Entries of the argument set a cached batch graph was captured with.
-constexpr int kGraphKey = 12;
+constexpr int kGraphKey = 15;
 
 struct rg_waveguide {
   rg_params p{};
@@ -206,6 +206,18 @@ struct rg_waveguide {
   // arguments (sizes, buffers, workspace, kernel choice) stay the same.
   cudaGraphExec_t graph = nullptr;
   int64_t graph_key[kGraphKey] = {0};
+  // rg_tdistrib_multi with this handle first: its device buffers (kept for
+  // the next call), one stream per kernel class, and the class launches
+  // captured as one CUDA graph (parallel branches), replayed while the
+  // launch plans and buffers stay the same.
+  static constexpr int kMultiClasses = 4;
+  void* d_multi = nullptr;
+  size_t multi_bytes = 0;
+  cudaStream_t multi_streams[kMultiClasses] = {};
+  cudaEvent_t multi_fork = nullptr, multi_join[kMultiClasses] = {};
+  cudaGraphExec_t multi_graph = nullptr;
+  std::vector<int64_t> multi_key;
+  int multi_replays = 0;
 };
 
 namespace {
@@ -237,6 +249,20 @@ void free_device(rg_waveguide* w) {
   cudaFree(w->d_scratch);
   if (w->graph) cudaGraphExecDestroy(w->graph);
   w->graph = nullptr;
+  if (w->multi_graph) cudaGraphExecDestroy(w->multi_graph);
+  w->multi_graph = nullptr;
+  w->multi_key.clear();
+  cudaFree(w->d_multi);
+  w->d_multi = nullptr;
+  w->multi_bytes = 0;
+  for (int c = 0; c < rg_waveguide::kMultiClasses; ++c) {
+    if (w->multi_streams[c]) cudaStreamDestroy(w->multi_streams[c]);
+    if (w->multi_join[c]) cudaEventDestroy(w->multi_join[c]);
+    w->multi_streams[c] = nullptr;
+    w->multi_join[c] = nullptr;
+  }
+  if (w->multi_fork) cudaEventDestroy(w->multi_fork);
+  w->multi_fork = nullptr;
   if (w->ev_sweep0) cudaEventDestroy(w->ev_sweep0);
   if (w->ev_sweep1) cudaEventDestroy(w->ev_sweep1);
   w->ev_sweep0 = w->ev_sweep1 = nullptr;
@@ -481,20 +507,29 @@ int place_workspace(rg_waveguide* w, rg::SweepArgs& a, size_t off, int* grid) {
 }
 
 // ---------------------------------------------------------------------------
-// Autotuner.  For a waveguide shape (M, ny) and a batch size, the candidate
-// launch configurations -- the blocked kernel's cluster size (CTAs per
-// realization), above 64 modes -- are timed once on a short proxy guide (the same modes and grid, 16
-// slices, the same number of realizations) and the fastest is cached for the
-// process.  RG_AUTOTUNE=0 disables it (the built-in heuristics decide).
-// Only choices that leave every realization's result bit for bit the same
-// are tuned: the cluster size changes which CTA computes an element, not its
-// arithmetic.  The kernel itself (symmetric for Dirichlet guides of up to 64
-// modes, pivoted shared-memory for periodic ones, blocked above 64 modes) is
-// fixed, so a realization gives the same bits in a batch of any size and in
-// a single call.
+// Autotuner.  For a waveguide shape (M, ny) and a batch size, candidate launch
+// configurations are timed once on a short proxy guide (the same modes and
+// grid, 16 slices, the same number of realizations) and the fastest is
+// cached for the process.  RG_AUTOTUNE=0 disables it (the built-in
+// heuristics decide).  Only choices that leave every realization's result
+// bit for bit the same are tuned:
+//   * above 64 modes, the blocked kernel's cluster size (CTAs per
+//     realization; it changes which CTA computes an element, not its
+//     arithmetic), then, for the chosen cluster size, the threads per update
+//     unit of the symmetric kernel (1, 4 or 8; it changes which thread
+//     updates a row, not the row's operations);
+//   * up to 64 modes, the persistent CTAs per SM of the shared-memory
+//     kernels (each realization is one CTA's, whatever the grid).
+// The kernel itself (symmetric for Dirichlet guides, pivoted shared-memory
+// for periodic ones up to 64 modes, blocked above) and the panel width of the
+// blocked elimination (8; another width regroups the rank updates and
+// changes the rounding) are fixed, so a realization gives the same bits in a
+// batch of any size and in a single call.
 // ---------------------------------------------------------------------------
 struct TuneChoice {
   int force_cluster = 0;
+  int force_rowsplit = 0;
+  int force_per_sm = 0;
 };
 
 struct TuneKey {
@@ -518,11 +553,17 @@ int size_bucket(int n) {
   return b;
 }
 
+void apply_choice(rg::SweepArgs& a, const TuneChoice& tc) {
+  a.force_cluster = tc.force_cluster;
+  a.force_rowsplit = tc.force_rowsplit;
+  a.force_per_sm = tc.force_per_sm;
+}
+
 // Times one configuration on the proxy (ms); large values mean "unusable".
 // seg_end > 0 stops the (blocked-kernel) sweep after that many slices, before
-// the Fisher-Lee and eigenvalue stage.
+// the Fisher-Lee and eigenvalue stage.  *grid_out receives the planned grid.
 double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const int32_t* d_seeds, double* d_teig,
-                      int32_t* d_status, const TuneChoice& tc, int seg_end, cudaStream_t s) {
+                      int32_t* d_status, const TuneChoice& tc, int seg_end, cudaStream_t s, int* grid_out = nullptr) {
   rg::SweepArgs a = make_args(w, rg::kModeEig);
   a.wgs = d_proxy;
   a.nreal = n;
@@ -530,10 +571,11 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
-  a.force_cluster = tc.force_cluster;
+  apply_choice(a, tc);
   int grid = 0;
   int64_t stride = 0;
   if (rg::sweep_plan(a, w->sm_count, &grid, &stride) != RG_OK) return 1e30;
+  if (grid_out) *grid_out = grid;
   const size_t need = align256(sizeof(double2) * (size_t)stride * (grid / (a.cluster > 0 ? a.cluster : 1)));
   double2* ws = nullptr;
   if (cudaMalloc((void**)&ws, need + sizeof(int32_t) * (size_t)n) != cudaSuccess) {
@@ -563,29 +605,23 @@ double time_candidate(rg_waveguide* w, const rg::WgDesc* d_proxy, int n, const i
 
 TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   TuneChoice def;
-  if (!autotune_enabled() || n <= 0 || w->nmu <= rg::kMaxModesSmem) return def;
+  if (!autotune_enabled() || n <= 0) return def;
+  const bool blocked = w->nmu > rg::kMaxModesSmem;
   const TuneKey key{w->nmu, w->ny, size_bucket(n), w->sm_count};
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) return it->second;
   }
-  std::vector<TuneChoice> cands;
-  for (int c = 1; c <= 8; c *= 2) cands.push_back(TuneChoice{c});
-  if (cands.size() == 1) {
-    std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache[key] = cands[0];
-    return cands[0];
-  }
-  // Proxy: the same waveguide cut to 16 slices (all disordered), stopped
-  // before the eigenvalue stage: at the sizes that reach the blocked kernel
-  // that stage is a negligible part of a real guide but would dominate 16
-  // slices.
+  // Proxy: the same waveguide cut to 16 slices (all disordered).  The
+  // blocked kernel stops before the eigenvalue stage (at the sizes that reach
+  // it that stage is a negligible part of a real guide but would dominate 16
+  // slices); the shared-memory kernels run whole guides.
   rg::WgDesc pd = w->h_desc;
   pd.nx = std::min(pd.nx, 16) + 1;
   pd.nxfree = 0;
   pd.nxdiso = pd.nx;
-  const int seg_end = pd.nx - 1;
+  const int seg_end = blocked ? pd.nx - 1 : 0;
   const int np = std::min(n, 4 * w->sm_count);
   char* buf = nullptr;
   const size_t b_desc = align256(sizeof pd), b_seed = align256(sizeof(int32_t) * np);
@@ -602,13 +638,34 @@ TuneChoice autotune(rg_waveguide* w, int n, cudaStream_t s) {
   for (int k = 0; k < np; ++k) seeds[k] = k + 1;
   cudaMemcpyAsync(d_pd, &pd, sizeof pd, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice, s);
-  TuneChoice best = cands[0];
+  TuneChoice best = def;
   double tbest = 1e30;
-  for (const TuneChoice& c : cands) {
-    const double t = time_candidate(w, d_pd, np, d_seeds, d_teig, d_status, c, seg_end, s);
+  auto consider = [&](const TuneChoice& c, int* grid_out = nullptr) {
+    const double t = time_candidate(w, d_pd, np, d_seeds, d_teig, d_status, c, seg_end, s, grid_out);
     if (t < tbest) {
       tbest = t;
       best = c;
+    }
+  };
+  if (blocked) {
+    for (int c = 1; c <= 8; c *= 2) consider(TuneChoice{c, 0, 0});
+    const int cbest = best.force_cluster;
+    if (w->p.boundtype == RG_BOUND_DIRICHLET)  // the symmetric kernel's row split
+      for (int t : {1, 4, 8}) consider(TuneChoice{cbest, t, 0});
+  } else {
+    // CTAs per SM: the occupancy limit, then fewer (distinct grids only)
+    std::vector<int> grids;
+    for (int k : {0, 1, 2, 4}) {
+      int gk = 0;
+      rg::SweepArgs a = make_args(w, rg::kModeEig);
+      a.wgs = d_pd;
+      a.nreal = np;
+      a.force_per_sm = k;
+      int64_t stride = 0;
+      if (rg::sweep_plan(a, w->sm_count, &gk, &stride) != RG_OK) continue;
+      if (std::find(grids.begin(), grids.end(), gk) != grids.end()) continue;
+      grids.push_back(gk);
+      consider(TuneChoice{0, 0, k});
     }
   }
   cudaStreamSynchronize(s);
@@ -632,7 +689,7 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   a.seeds = d_seeds;
   a.teig = d_teig;
   a.status = d_status;
-  a.force_cluster = tc.force_cluster;
+  apply_choice(a, tc);
   int grid = 0, rc;
   if ((rc = place_workspace(w, a, 0, &grid))) return rc;
   int64_t tau_bits = 0;
@@ -640,7 +697,7 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   const int64_t key[kGraphKey] = {n, (int64_t)(intptr_t)d_seeds, (int64_t)(intptr_t)d_teig,
                                   (int64_t)(intptr_t)d_status, (int64_t)(intptr_t)a.work, grid, a.cluster,
                                   a.force_large, a.work_stride, a.symmetric, (int64_t)(intptr_t)a.flag_list,
-                                  tau_bits};
+                                  tau_bits, a.force_rowsplit, a.force_per_sm, a.tensor_r};
   if (!w->graph || std::memcmp(key, w->graph_key, sizeof key) != 0) {
     if (w->graph) cudaGraphExecDestroy(w->graph);
     w->graph = nullptr;
@@ -1147,26 +1204,47 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
   }
   DeviceGuard g(w0->device);
   cudaStream_t s = w0->stream;
+  // Device buffers, kept on w0 for the next call (grow-only): descriptors,
+  // item waveguides, seeds, statuses, output offsets, outputs, and the queue
+  // counters of each class.
   const size_t b_desc = align256(sizeof(rg::WgDesc) * descs.size()), b_i32 = align256(sizeof(int32_t) * n);
   const size_t b_off = align256(sizeof(int64_t) * n), b_out = align256(sizeof(double) * (size_t)len);
-  char* dbuf = nullptr;
-  RG_CUDA(cudaMalloc((void**)&dbuf, b_desc + 3 * b_i32 + b_off + b_out));
+  const size_t b_cnt = align256(sizeof(int) * rg::kQueueCounters * rg_waveguide::kMultiClasses);
+  const size_t need = b_desc + 3 * b_i32 + b_off + b_out + b_cnt;
+  if (need > w0->multi_bytes) {
+    if (w0->multi_graph) cudaGraphExecDestroy(w0->multi_graph);
+    w0->multi_graph = nullptr;
+    w0->multi_key.clear();
+    cudaFree(w0->d_multi);
+    w0->d_multi = nullptr;
+    w0->multi_bytes = 0;
+    cudaError_t e = cudaMalloc(&w0->d_multi, need);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return rg::fail(RG_ERR_NOMEM, "rg_tdistrib_multi: device allocation of " + std::to_string(need) + " bytes failed");
+    }
+    w0->multi_bytes = need;
+  }
+  char* dbuf = (char*)w0->d_multi;
   rg::WgDesc* d_desc = (rg::WgDesc*)dbuf;
   int32_t* d_wg = (int32_t*)(dbuf + b_desc);
   int32_t* d_seed = (int32_t*)(dbuf + b_desc + b_i32);
   int32_t* d_st = (int32_t*)(dbuf + b_desc + 2 * b_i32);
   int64_t* d_off = (int64_t*)(dbuf + b_desc + 3 * b_i32);
   double* d_out = (double*)(dbuf + b_desc + 3 * b_i32 + b_off);
-  std::vector<int32_t> st_sorted(n);
+  int* d_cnt = (int*)(dbuf + b_desc + 3 * b_i32 + b_off + b_out);
+
+  // One persistent launch per kernel class, each with its own workspace and
+  // queue counters, so that the classes can run side by side.
+  struct Cls {
+    rg::SweepArgs a;
+    int grid;
+    size_t ws_off, ws_bytes;
+  };
+  std::vector<Cls> cls;
+  size_t total_ws = 0;
   int rc = RG_OK;
-  cudaError_t e = cudaMemcpyAsync(d_desc, descs.data(), sizeof(rg::WgDesc) * descs.size(), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_wg, o_wg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seed, o_seed.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, o_off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)len, s);
-  if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi upload");
-  // One persistent launch per kernel class.
-  for (int k0 = 0; !rc && k0 < n;) {
+  for (int k0 = 0; k0 < n;) {
     const int cl = klass(descs[o_wg[k0]].M);
     int k1 = k0, maxM = 0, maxny = 0;
     while (k1 < n && klass(descs[o_wg[k1]].M) == cl) {
@@ -1183,7 +1261,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     a.teig_off = d_off + k0;
     a.teig = d_out;
     a.status = d_st + k0;
-    a.work_counter = w0->d_counter;
+    a.work_counter = d_cnt + cls.size() * rg::kQueueCounters;
     a.max_M = maxM;
     a.max_ny = maxny;
     // The symmetric kernel when the class has Dirichlet items (it hands
@@ -1210,25 +1288,87 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
       while (C < 8 && longest * slots / C > total) C *= 2;
       a.force_cluster = C > 1 ? C : 0;
     }
-    int grid = 0;
-    if ((rc = place_workspace(w0, a, 0, &grid))) break;
-    e = cudaMemsetAsync(w0->d_counter, 0, sizeof(int) * rg::kQueueCounters, s);
-    if (e != cudaSuccess) {
-      rc = rg::cuda_fail(e, "rg_tdistrib_multi counter");
-      break;
-    }
-    if ((rc = rg::launch_sweep(a, s, grid))) break;
+    Cls c{a, 0, 0, 0};
+    int64_t stride = 0;
+    if ((rc = rg::sweep_plan(c.a, w0->sm_count, &c.grid, &stride))) return rc;
+    c.a.work_stride = stride;
+    const size_t ws = align256(sizeof(double2) * (size_t)stride * (c.grid / (c.a.cluster > 0 ? c.a.cluster : 1)));
+    const size_t fl = c.a.symmetric ? align256(sizeof(int32_t) * (size_t)c.a.nreal) : 0;
+    c.ws_off = total_ws;
+    c.ws_bytes = ws;
+    total_ws += ws + fl;
+    cls.push_back(c);
     k0 = k1;
   }
-  if (!rc) {
-    e = cudaMemcpyAsync(tallvals, d_out, sizeof(double) * (size_t)len, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(st_sorted.data(), d_st, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi");
+  if ((rc = ensure_scratch(w0, total_ws))) return rc;
+  for (Cls& c : cls) {
+    c.a.work = (double2*)((char*)w0->d_scratch + c.ws_off);
+    c.a.flag_list = c.a.symmetric ? (int32_t*)((char*)w0->d_scratch + c.ws_off + c.ws_bytes) : nullptr;
   }
-  cudaStreamSynchronize(s);
-  cudaFree(dbuf);
-  if (rc) return rc;
+  // Inputs for this call (outside the graph, which reads them from the buffers).
+  cudaError_t e = cudaMemcpyAsync(d_desc, descs.data(), sizeof(rg::WgDesc) * descs.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_wg, o_wg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seed, o_seed.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, o_off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)len, s);
+  if (e != cudaSuccess) return rg::cuda_fail(e, "rg_tdistrib_multi upload");
+  // The graph: counters reset, then every class on its own stream.
+  std::vector<int64_t> key = {n, len, (int64_t)(intptr_t)w0->d_multi, (int64_t)(intptr_t)w0->d_scratch,
+                              (int64_t)descs.size(), (int64_t)cls.size()};
+  for (const Cls& c : cls) {
+    int64_t tau_bits = 0;
+    std::memcpy(&tau_bits, &c.a.sym_tau, sizeof tau_bits);
+    const int64_t k[] = {(int64_t)(c.a.item_wg - d_wg), c.a.nreal, c.a.max_M, c.a.max_ny, c.a.symmetric,
+                         c.a.tensor_r, c.a.force_cluster, c.a.cluster, c.grid, (int64_t)c.ws_off, c.a.work_stride,
+                         tau_bits};
+    key.insert(key.end(), std::begin(k), std::end(k));
+  }
+  if (!w0->multi_graph || key != w0->multi_key) {
+    if (w0->multi_graph) cudaGraphExecDestroy(w0->multi_graph);
+    w0->multi_graph = nullptr;
+    w0->multi_key.clear();
+    if (!w0->multi_fork) RG_CUDA(cudaEventCreateWithFlags(&w0->multi_fork, cudaEventDisableTiming));
+    for (size_t c = 0; c < cls.size(); ++c) {
+      if (!w0->multi_streams[c]) RG_CUDA(cudaStreamCreateWithFlags(&w0->multi_streams[c], cudaStreamNonBlocking));
+      if (!w0->multi_join[c]) RG_CUDA(cudaEventCreateWithFlags(&w0->multi_join[c], cudaEventDisableTiming));
+    }
+    cudaGraph_t gr = nullptr;
+    RG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    e = cudaMemsetAsync(d_cnt, 0, b_cnt, s);
+    if (e == cudaSuccess) e = cudaEventRecord(w0->multi_fork, s);
+    if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi capture");
+    for (size_t c = 0; !rc && c < cls.size(); ++c) {
+      cudaStream_t sc = w0->multi_streams[c];
+      e = cudaStreamWaitEvent(sc, w0->multi_fork, 0);
+      if (e != cudaSuccess) {
+        rc = rg::cuda_fail(e, "rg_tdistrib_multi capture");
+        break;
+      }
+      if ((rc = rg::launch_sweep(cls[c].a, sc, cls[c].grid))) break;
+      e = cudaEventRecord(w0->multi_join[c], sc);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, w0->multi_join[c], 0);
+      if (e != cudaSuccess) rc = rg::cuda_fail(e, "rg_tdistrib_multi capture");
+    }
+    const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+    if (rc) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    RG_CUDA(ec);
+    e = cudaGraphInstantiate(&w0->multi_graph, gr, 0);
+    cudaGraphDestroy(gr);
+    RG_CUDA(e);
+    w0->multi_key = key;
+    w0->multi_replays = 0;
+  } else {
+    ++w0->multi_replays;
+  }
+  std::vector<int32_t> st_sorted(n);
+  e = cudaGraphLaunch(w0->multi_graph, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tallvals, d_out, sizeof(double) * (size_t)len, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(st_sorted.data(), d_st, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return rg::cuda_fail(e, "rg_tdistrib_multi");
   int bad = RG_OK;
   for (int k = 0; k < n; ++k) {
     if (status) status[order[k]] = st_sorted[k];

@@ -123,3 +123,81 @@ def test_c5short_closed_channels():
         # Weyl with 4x the sketch estimate (a 4-vector estimate is within a
         # factor 2 of ||D||_F with overwhelming probability)
         assert np.all(weyl_ok(Tg, To, 4 * dt_est, np.sqrt(To[0]))), s
+
+
+def _allowed_tie_bins(samples, edges, tol=1e-9):
+    """Bins whose count may differ between two computations of the same
+    samples: those on either side of an edge that a sample lies within tol of."""
+    bins = set()
+    for x in samples:
+        k = np.searchsorted(edges, x)
+        for e in (k - 1, k):
+            if 0 <= e < len(edges) and abs(x - edges[e]) <= tol:
+                bins.update((e - 1, e))
+    return bins
+
+
+def test_c3_costliest_uneven_items():
+    """The 8 costliest guides of the batched-uneven workload (N = 256, Nx ~ 4900
+    to 5000 slices, three with absorption eps = 0.01 k^2, i.e. complex sqrt(mu)
+    in Fisher-Lee), each with its own L/l_s and seed, in one size-grouped
+    rg_tdistrib_multi call, against oracle fixtures: T_n within 1e-9, and the
+    Chebyshev histogram counts of the tdistrib task (100 bins) equal except in
+    the two bins beside an edge a value lies within 1e-9 of.  Two of them (one
+    absorbing) also through the caller-given-potential path, for t itself."""
+    from golden.make_large_fixtures import SKETCH_K, c3_top8, sketch_vectors
+    from recurgreen_gb300.tdistrib import chebyshev_bins
+
+    f = _fixture("c3top8")
+    items = c3_top8()
+    assert [s for _, s in items] == list(f["seeds"])
+    gs = [rg.Waveguide(**kw) for kw, _ in items]
+    res = rg.tdistrib_multi([(g, int(s)) for g, (_, s) in zip(gs, items)])
+    To_all, Tg_all = [], []
+    for k, (T, (kw, s)) in enumerate(zip(res, items)):
+        To = f["T"][k]
+        assert np.max(np.abs(T - To)) <= TN_ABS, (s, kw)
+        To_all.append(To)
+        Tg_all.append(T)
+    edges = chebyshev_bins(100)
+    hg, mg = rg.histogram(np.concatenate(Tg_all), edges)
+    ho, mo = O.histogram(np.concatenate(To_all), edges)
+    diff = set(np.nonzero(np.asarray(hg) != np.asarray(ho))[0].tolist())
+    assert diff <= _allowed_tie_bins(np.concatenate(To_all), edges), diff
+    assert mg == mo
+    absorbing = [k for k, (kw, _) in enumerate(items) if kw["dabso"] > 0]
+    plain = [k for k, (kw, _) in enumerate(items) if kw["dabso"] == 0]
+    for k in (absorbing[0], plain[0]):
+        kw, s = items[k]
+        o = O.Waveguide(**kw)
+        Tg, tg = gs[k].tdistrib_upot(o.potential(s), want_t=True)
+        dt_est = np.linalg.norm(tg @ sketch_vectors(tg.shape[1]) - f["sketch"][k]) / np.sqrt(SKETCH_K)
+        assert dt_est / f["tnorm"][k] <= T_REL, s
+        assert np.all(weyl_ok(Tg, f["T"][k], 4 * dt_est, np.sqrt(f["T"][k][0]))), s
+
+
+def test_adjoint_fd_at_differentiation_config():
+    """The differentiation configuration itself (M = 128, kW/pi = 128.5, Nx =
+    1000, ny = 512, L/l_s = 5), seeds 1 and 2, 64 random grid cells each: both
+    gradients from one backward pass against the oracle's central finite
+    differences (step 1e-6 sigma_U, fixtures from make_large_fixtures.py
+    difffd), within 1e-6 of the largest sampled finite difference; the losses
+    within 1e-10 of the oracle's."""
+    torch = pytest.importorskip("torch")
+    from golden.make_large_fixtures import DIFF_KW
+    from recurgreen_gb300.adjoint import transmission_losses_and_grads
+
+    f = _fixture("difffd")
+    o, g = O.Waveguide(**DIFF_KW), rg.Waveguide(**DIFF_KW)
+    us = [o.potential(int(s)) for s in f["seeds"]]
+    U = torch.tensor(np.stack([u.T for u in us]), dtype=torch.float64, device="cuda")
+    L1, L2, g1, g2 = transmission_losses_and_grads(U, g)
+    L = np.stack([L1.cpu().numpy(), L2.cpu().numpy()], axis=1)
+    assert np.all(np.abs(L - f["losses"]) <= 1e-10 * np.abs(f["losses"]))
+    for k, grad in enumerate((g1.cpu().numpy(), g2.cpu().numpy())):
+        for r in range(len(us)):
+            cells = f["cells"][r]
+            fd = f["fd"][r, :, k]
+            adj = grad[r, cells[:, 0], cells[:, 1]]
+            err = np.max(np.abs(adj - fd)) / np.max(np.abs(fd))
+            assert err <= 1e-6, (k, r, err)
