@@ -462,6 +462,20 @@ def run_workload(args) -> None:
         out["frac_of_fp64_peak"] = out["dense_equivalent_tflops"] / peak
         T = T.reshape(n, w.neigv)
         out["smallest_T"] = float(T.min())
+        fix = os.path.join(ROOT, "tests", "golden", "oracle_c5.npz")
+        if w.nx == 10000 and w.ny == 2048 and os.path.exists(fix):
+            # the oracle's eigenvalues of seeds 1..16 (tests/golden/make_large_fixtures.py c5)
+            f = np.load(fix)
+            k = [int(s) - 1 for s in f["seeds"] if s <= n]
+            if k:
+                To, Tg = f["T"][: len(k)], T[k]
+                big = To >= 1e-12
+                out["parity_vs_oracle"] = {
+                    "seeds": [int(s) for s in f["seeds"][: len(k)]],
+                    "max_abs_T_err": float(np.max(np.abs(Tg - To))),
+                    "max_rel_T_err_for_T_ge_1e-12": float(np.max(np.abs(Tg - To)[big] / To[big])),
+                    "eigenvalues_with_T_ge_1e-12": int(big.sum()),
+                    "smallest_oracle_T": float(To.min())}
         if args.per_sample > 0:
             pr, pdt = _per_realization(L, w, list(range(1, args.per_sample + 1)), np)
             out["per_realization_per_s"] = pr

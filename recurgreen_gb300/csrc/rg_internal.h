@@ -135,6 +135,11 @@ struct SweepArgs {
   // of carrying B Gs1 through the Gauss-Jordan sweep (up to 512 modes).
   // Set from RG_TENSOR_R (default on).
   int tensor_r;
+  // 1 (with tensor_r): above 127 modes, even mode counts, the blocked
+  // symmetric kernel inverts X in its 2 x 2 block form, two half-size FP64
+  // Gauss-Jordan sweeps and four half-size tensor-core products.  Set from
+  // RG_SPLIT_INVERSE (default on).
+  int split_inverse;
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were
@@ -224,6 +229,7 @@ struct GreenView {
   int symmetric;         // the symmetric sweep is enabled for this guide (Dirichlet)
   double sym_tau;        // its pivot threshold
   int tensor_r;          // SweepArgs::tensor_r for this guide
+  int split_inverse;     // SweepArgs::split_inverse for this guide
 };
 int green_view(const rg_waveguide* w, GreenView* out);
 

@@ -56,6 +56,8 @@ constexpr int kSymNT = 256;
 constexpr int kSymNB = 8;
 constexpr int kSymMaxCluster = 8;
 constexpr int kSymMaxRowSplit = 8;
+// The 2 x 2 block inverse for even mode counts from this size up.
+constexpr int kSplitMinModes = 128;
 
 // The pivot column (panel phase) and the chunk's z values (update phase)
 // share one region: they are never live at the same time.
@@ -93,11 +95,14 @@ __host__ __device__ inline int64_t large_sym_base_stride(int M, int ny) {
   const int64_t urow = ((int64_t)ny + 1) / 2;
   return ((3 * mm + 2 * (int64_t)ny + urow + (int64_t)kSymMaxCluster * kSymNB * M) + 15) & ~(int64_t)15;
 }
-inline int64_t large_sym_stride(int M, int ny, bool tensor) {
-  const int64_t base = large_sym_base_stride(M, ny);
-  if (!tensor) return base;
+// Then the 2 x 2 block inverse's three h x h buffers (h = M / 2).
+__host__ __device__ inline int64_t large_sym_schur_offset(int M, int ny) {
   const int64_t ex = ((int64_t)kSymMaxCluster * 2 * 16 * oz::tiles(M) * 4 + 15) / 16;
-  return (base + 2 * oz::operand_uint4(M) + ex + 15) & ~(int64_t)15;
+  return (large_sym_base_stride(M, ny) + 2 * oz::operand_uint4(M) + ex + 15) & ~(int64_t)15;
+}
+inline int64_t large_sym_stride(int M, int ny, bool tensor) {
+  if (!tensor) return large_sym_base_stride(M, ny);
+  return (large_sym_schur_offset(M, ny) + 3 * (int64_t)(M / 2) * (M / 2) + 15) & ~(int64_t)15;
 }
 
 __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
@@ -203,6 +208,11 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
     uint4* adig = reinterpret_cast<uint4*>(ws + large_sym_base_stride(M, ny));  // product digit planes
     uint4* bdig = adig + oz::operand_uint4(M);
     int* expart = reinterpret_cast<int*>(bdig + oz::operand_uint4(M));  // [C][2][16 T] partial exponents
+    // the 2 x 2 block inverse's buffers: A^-1, T = A^-1 B, S^-1 (h x h each)
+    const bool split = gemm_on && a.split_inverse && M >= kSplitMinModes && (M % 2) == 0;
+    double2* Wa = ws + large_sym_schur_offset(M, ny);
+    double2* Tb = Wa + (int64_t)(M / 2) * (M / 2);
+    double2* Ws = Tb + (int64_t)(M / 2) * (M / 2);
     if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
     const double one = a.inject_at > 0 ? 0.0 : 1.0;  // the source at slice 0, or zero until inject_at
     for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? one : 0.0, 0.0);
@@ -309,276 +319,394 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
                                      : cmul(wd.bmat[i], cscale(rsign, __ldcg(Rg + e)));
       }
       cluster.sync();
-      unsigned long long best = 0ULL;
-      int bi = 0x7fffffff;
-      for (int i = tid; i < M; i += NT) {
-        const double2 x = __ldcg(W + (int64_t)i * M + i);
-        dg[i] = x;
-        used[i] = 0;
-        const unsigned long long k = pivot_key(x);
-        if (k > best) {
-          best = k;
-          bi = i;
+      // 3. Blocked symmetric Gauss-Jordan of the M x M symmetric matrix whose
+      //    upper triangle is stored at W (row stride M): W becomes its inverse
+      //    (and, without the tensor-core product, the R columns Rg become
+      //    X^-1 Rg).  Ends with a cluster barrier.
+      auto gj = [&](double2* W, const int M) {
+        unsigned long long best = 0ULL;
+        int bi = 0x7fffffff;
+        for (int i = tid; i < M; i += NT) {
+          const double2 x = __ldcg(W + (int64_t)i * M + i);
+          dg[i] = x;
+          used[i] = 0;
+          const unsigned long long k = pivot_key(x);
+          if (k > best) {
+            best = k;
+            bi = i;
+          }
         }
-      }
-      reduce_pivot(best, bi, 0ULL);
+        reduce_pivot(best, bi, 0ULL);
 
-      // 3. Blocked symmetric Gauss-Jordan.
-      for (int k0 = 0; k0 < M; k0 += NB) {
-        const int nbk = min(NB, M - k0);
-        for (int i = tid; i < M; i += NT) used0[i] = used[i];
-        __syncthreads();
-        for (int kk = 0; kk < nbk; ++kk) {
-          int p = s_p;
-          if (p < 0) {  // zero or NaN diagonal everywhere left: the pivoted kernel decides
-            if (tid == 0) s_status = kStatusNeedPivot;
-            p = 0;
-            while (p < M - 1 && used[p]) ++p;
-          }
-          // a. column p at the panel start: W[i][p] above the diagonal, and
-          //    below it M[i][p] = +-W[p][i], minus when i was swept before the panel
-          for (int i = tid; i < M; i += NT) {
-            double2 v;
-            if (i <= p) {
-              v = __ldcg(W + (int64_t)i * M + p);
-            } else {
-              v = __ldcg(W + (int64_t)p * M + i);
-              if (used0[i]) v = cneg(v);
-            }
-            PR[(int64_t)kk * M + i] = v;
-            colb[i] = v;
-          }
+        // 3. Blocked symmetric Gauss-Jordan.
+        for (int k0 = 0; k0 < M; k0 += NB) {
+          const int nbk = min(NB, M - k0);
+          for (int i = tid; i < M; i += NT) used0[i] = used[i];
           __syncthreads();
-          if (kk > 0) {
-            // b. the panel's earlier steps: z_m = x[p_m] + sum_{l<m} u_l[p_m] z_l, x += U z
-            if (tid == 0) {
-              for (int m = 0; m < kk; ++m) {
-                const int pm = piv[k0 + m];
-                double2 v = colb[pm];
-                for (int l = 0; l < m; ++l) v = cfms(v, cneg(Ub[pm * NB + l]), zc[l]);
-                zc[m] = v;
-              }
+          for (int kk = 0; kk < nbk; ++kk) {
+            int p = s_p;
+            if (p < 0) {  // zero or NaN diagonal everywhere left: the pivoted kernel decides
+              if (tid == 0) s_status = kStatusNeedPivot;
+              p = 0;
+              while (p < M - 1 && used[p]) ++p;
             }
-            __syncthreads();
+            // a. column p at the panel start: W[i][p] above the diagonal, and
+            //    below it M[i][p] = +-W[p][i], minus when i was swept before the panel
             for (int i = tid; i < M; i += NT) {
-              double2 x = colb[i];
-              for (int m = 0; m < kk; ++m) x = cfms(x, cneg(Ub[i * NB + m]), zc[m]);
-              colb[i] = x;
+              double2 v;
+              if (i <= p) {
+                v = __ldcg(W + (int64_t)i * M + p);
+              } else {
+                v = __ldcg(W + (int64_t)p * M + i);
+                if (used0[i]) v = cneg(v);
+              }
+              PR[(int64_t)kk * M + i] = v;
+              colb[i] = v;
+            }
+            __syncthreads();
+            if (kk > 0) {
+              // b. the panel's earlier steps: z_m = x[p_m] + sum_{l<m} u_l[p_m] z_l, x += U z
+              if (tid == 0) {
+                for (int m = 0; m < kk; ++m) {
+                  const int pm = piv[k0 + m];
+                  double2 v = colb[pm];
+                  for (int l = 0; l < m; ++l) v = cfms(v, cneg(Ub[pm * NB + l]), zc[l]);
+                  zc[m] = v;
+                }
+              }
+              __syncthreads();
+              for (int i = tid; i < M; i += NT) {
+                double2 x = colb[i];
+                for (int m = 0; m < kk; ++m) x = cfms(x, cneg(Ub[i * NB + m]), zc[m]);
+                colb[i] = x;
+              }
+              __syncthreads();
+            }
+            // c. reciprocal, multipliers, diagonal update; the next pivot and the
+            //    largest unswept entry of this column in one reduction
+            const double2 z = colb[p];
+            const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
+            const double2 d = make_double2(z.x * rden, -z.y * rden);
+            unsigned long long nbest = 0ULL, cm = 0ULL;
+            int nbi = 0x7fffffff;
+            for (int i = tid; i < M; i += NT) {
+              const double2 g = colb[i];
+              double2 u;
+              if (i == p) {
+                u = make_double2(d.x - 1.0, d.y);
+              } else {
+                u = cneg(cmul(g, d));
+              }
+              Ub[i * NB + kk] = u;
+              if (!used[i] && i != p) {
+                const unsigned long long kc = pivot_key(g);
+                cm = kc > cm ? kc : cm;
+                const double2 nd2 = cfms(dg[i], cneg(u), g);  // dg + u g
+                dg[i] = nd2;
+                const unsigned long long kd = pivot_key(nd2);
+                if (kd > nbest) {
+                  nbest = kd;
+                  nbi = i;
+                }
+              }
+            }
+            reduce_pivot(nbest, nbi, cm);
+            if (tid == 0) {
+              const double zmag = __longlong_as_double((long long)pivot_key(z));
+              const double omag = __longlong_as_double((long long)s_cmax);
+              if (!(zmag > 0.0) || zmag < a.sym_tau * omag) s_status = kStatusNeedPivot;
+              used[p] = 1;
+              piv[k0 + kk] = p;
             }
             __syncthreads();
           }
-          // c. reciprocal, multipliers, diagonal update; the next pivot and the
-          //    largest unswept entry of this column in one reduction
-          const double2 z = colb[p];
-          const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
-          const double2 d = make_double2(z.x * rden, -z.y * rden);
-          unsigned long long nbest = 0ULL, cm = 0ULL;
-          int nbi = 0x7fffffff;
-          for (int i = tid; i < M; i += NT) {
-            const double2 g = colb[i];
-            double2 u;
-            if (i == p) {
-              u = make_double2(d.x - 1.0, d.y);
-            } else {
-              u = cneg(cmul(g, d));
-            }
-            Ub[i * NB + kk] = u;
-            if (!used[i] && i != p) {
-              const unsigned long long kc = pivot_key(g);
-              cm = kc > cm ? kc : cm;
-              const double2 nd2 = cfms(dg[i], cneg(u), g);  // dg + u g
-              dg[i] = nd2;
-              const unsigned long long kd = pivot_key(nd2);
-              if (kd > nbest) {
-                nbest = kd;
-                nbi = i;
-              }
-            }
+          for (int e = tid; e < nbk * nbk; e += NT) {
+            const int k = e / nbk, l = e % nbk;
+            Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
           }
-          reduce_pivot(nbest, nbi, cm);
-          if (tid == 0) {
-            const double zmag = __longlong_as_double((long long)pivot_key(z));
-            const double omag = __longlong_as_double((long long)s_cmax);
-            if (!(zmag > 0.0) || zmag < a.sym_tau * omag) s_status = kStatusNeedPivot;
-            used[p] = 1;
-            piv[k0 + kk] = p;
-          }
-          __syncthreads();
-        }
-        for (int e = tid; e < nbk * nbk; e += NT) {
-          const int k = e / nbk, l = e % nbk;
-          Lt[k * NB + l] = (l < k) ? Ub[piv[k0 + k] * NB + l] : make_double2(0.0, 0.0);
-        }
-        // The panel's column fetches read W anywhere (row p_k lies in other
-        // columns), so no CTA of the cluster may start writing W until every
-        // CTA has finished factoring the panel.
-        if (C > 1) cluster.sync();
-        else __syncthreads();
+          // The panel's column fetches read W anywhere (row p_k lies in other
+          // columns), so no CTA of the cluster may start writing W until every
+          // CTA has finished factoring the panel.
+          if (C > 1) cluster.sync();
+          else __syncthreads();
 
-        // d. The panel applied to every column of [W | R]: a column gets
-        //    x += U z over its rows (i <= j for W, all for R), with
-        //    z = (I - L)^-1 x[p] from its pivot rows (for W, the panel's raw
-        //    pivot columns with the sign rule), and the panel's pivot column
-        //    m is u_m + e_{p_m} with the later steps applied.
-        auto column_z = [&](int kind, int j, int mcol, const double2* col, double2* zz) {
-#pragma unroll
-          for (int k = 0; k < NB; ++k) zz[k] = make_double2(0.0, 0.0);
-          if (kind == 1) {
-#pragma unroll
-            for (int l = 0; l < NB; ++l) {
-              if (l > mcol && l < nbk) {
-                double2 v = Lt[l * NB + mcol];
-#pragma unroll
-                for (int q = 0; q < NB; ++q)
-                  if (q > mcol && q < l) v = cfms(v, cneg(Lt[l * NB + q]), zz[q]);
-                zz[l] = v;
+          // d. The panel applied to every column of [W | R]: a column gets
+          //    x += U z over its rows (i <= j for W, all for R), with
+          //    z = (I - L)^-1 x[p] from its pivot rows (for W, the panel's raw
+          //    pivot columns with the sign rule), and the panel's pivot column
+          //    m is u_m + e_{p_m} with the later steps applied.
+          auto column_z = [&](int kind, int j, int mcol, const double2* col, double2* zz) {
+  #pragma unroll
+            for (int k = 0; k < NB; ++k) zz[k] = make_double2(0.0, 0.0);
+            if (kind == 1) {
+  #pragma unroll
+              for (int l = 0; l < NB; ++l) {
+                if (l > mcol && l < nbk) {
+                  double2 v = Lt[l * NB + mcol];
+  #pragma unroll
+                  for (int q = 0; q < NB; ++q)
+                    if (q > mcol && q < l) v = cfms(v, cneg(Lt[l * NB + q]), zz[q]);
+                  zz[l] = v;
+                }
               }
-            }
-          } else {
-            const double sg = (kind == 0 && used0[j]) ? -1.0 : 1.0;
-#pragma unroll
-            for (int m = 0; m < NB; ++m) {
-              if (m < nbk) {
-                double2 v = (kind == 0) ? cscale(sg, __ldcg(PR + (int64_t)m * M + j))
-                                        : __ldcg(col + (int64_t)piv[k0 + m] * M);
-#pragma unroll
-                for (int l = 0; l < m; ++l) v = cfms(v, cneg(Lt[m * NB + l]), zz[l]);
-                zz[m] = v;
-              }
-            }
-          }
-        };
-        // The rows of a unit as one sequence of virtual rows v = sub, sub+T,
-        // ... < lena + lenb: v < lena is row v of column a, the rest row
-        // v - lena of column b.  A pair unit has M+1 virtual rows and an R
-        // unit M, so the threads of a warp (consecutive units) run the same
-        // trip count and their FP64 instructions keep every lane busy.
-        struct Col {
-          int kind, j, mcol, len;
-          double2* col;
-        };
-        auto unit_rows = [&](const Col& A, const double2* za, const Col& B, const double2* zb, int sub, int T) {
-          const int tot = A.len + B.len;
-          // the starting value of virtual row v and where it goes
-          auto load = [&](int v, int* irow, double2** dst) {
-            const bool inA = v < A.len;
-            const Col& c = inA ? A : B;
-            const int i = inA ? v : v - A.len;
-            *irow = i;
-            *dst = c.col + (int64_t)i * M;
-            if (c.kind == 1) {
-              double2 x = Ub[i * NB + c.mcol];
-              if (i == c.j) x.x += 1.0;
-              return x;
-            }
-            return __ldcg(*dst);
-          };
-          int v = sub;
-          for (; v < tot; v += T) {
-            int i;
-            double2* d;
-            double2 x = load(v, &i, &d);
-            const bool a0 = v < A.len;
-            const double2* ui = Ub + i * NB;
-#pragma unroll
-            for (int k = 0; k < NB; ++k)
-              if (k < nbk) x = cfms(x, cneg(ui[k]), a0 ? za[k] : zb[k]);
-            *d = x;
-          }
-        };
-        // Which kind of W column j is: 1 if it is pivot mcol of this panel.
-        auto w_kind = [&](int j, int* mcol) {
-          *mcol = -1;
-          if (used[j] && !used0[j]) {
-            for (int m = 0; m < nbk; ++m)
-              if (piv[k0 + m] == j) *mcol = m;
-            return 1;
-          }
-          return 0;
-        };
-        // Units: the W column pairs (q, M-1-q), M+1 rows together, then the
-        // R columns (M rows), dealt round-robin to the cluster's CTAs.  T
-        // threads share a unit's rows (T = 1, 4 or 8, whichever gives the
-        // fewest rows per thread); with T > 1 the unit's z vectors (two for
-        // a pair) come through shared memory, [NT/4][2][NB] at most.
-        const int P = (M + 1) / 2;
-        const int ucta = (P + (gemm_on ? 0 : M) - rank + C - 1) / C;  // R columns only without the product
-        int T = 1;
-        if (a.force_rowsplit == 1 || a.force_rowsplit == 4 || a.force_rowsplit == 8) {
-          T = a.force_rowsplit;  // the autotuner's choice (the same arithmetic per element)
-        } else {
-          int best = ((ucta + NT - 1) / NT) * (M + 1);
-          for (int t = 4; t <= kSymMaxRowSplit; t *= 2) {
-            const int rows = ((ucta + NT / t - 1) / (NT / t)) * ((M + 1 + t - 1) / t);
-            if (rows < best) {
-              best = rows;
-              T = t;
-            }
-          }
-        }
-        const int NCH = NT / T;
-        const int cs = tid % NCH, sub = tid / NCH;
-        for (int c0 = 0; c0 < ucta; c0 += NCH) {
-          const int c = c0 + cs;
-          const bool active = c < ucta;
-          const int u = rank + C * c;
-          int ka = 0, kb = 0, ja = 0, jb = 0, ma = -1, mb = -1, lena = 0, lenb = 0;
-          double2* cola = nullptr;
-          double2* colb2 = nullptr;
-          if (active) {
-            if (u < P) {
-              ja = u;
-              jb = M - 1 - u;
-              lena = ja + 1;
-              lenb = (jb != ja) ? jb + 1 : 0;
-              cola = W + ja;
-              colb2 = W + jb;
-              ka = w_kind(ja, &ma);
-              if (lenb) kb = w_kind(jb, &mb);
             } else {
-              ka = 2;
-              ja = u - P;
-              lena = M;
-              cola = Rg + ja;
-            }
-          }
-          const Col A{ka, ja, ma, lena, cola};
-          const Col B{kb, jb, mb, lenb, colb2 ? colb2 : cola};
-          double2 za[NB], zb[NB];
-#pragma unroll
-          for (int k = 0; k < NB; ++k) zb[k] = make_double2(0.0, 0.0);
-          if (T == 1) {
-            if (active) {
-              column_z(ka, ja, ma, cola, za);
-              if (lenb) column_z(kb, jb, mb, colb2, zb);
-              unit_rows(A, za, B, zb, 0, 1);
-            }
-          } else {
-            if (active && sub < 2 && (sub == 0 || lenb)) {
-              double2 zz[NB];
-              if (sub == 0) column_z(ka, ja, ma, cola, zz);
-              else column_z(kb, jb, mb, colb2, zz);
-#pragma unroll
-              for (int k = 0; k < NB; ++k) zsh[(cs * 2 + sub) * NB + k] = zz[k];
-            }
-            __syncthreads();  // z is read before any row of these columns changes
-            if (active) {
-#pragma unroll
-              for (int k = 0; k < NB; ++k) za[k] = zsh[(cs * 2) * NB + k];
-              if (lenb) {
-#pragma unroll
-                for (int k = 0; k < NB; ++k) zb[k] = zsh[(cs * 2 + 1) * NB + k];
+              const double sg = (kind == 0 && used0[j]) ? -1.0 : 1.0;
+  #pragma unroll
+              for (int m = 0; m < NB; ++m) {
+                if (m < nbk) {
+                  double2 v = (kind == 0) ? cscale(sg, __ldcg(PR + (int64_t)m * M + j))
+                                          : __ldcg(col + (int64_t)piv[k0 + m] * M);
+  #pragma unroll
+                  for (int l = 0; l < m; ++l) v = cfms(v, cneg(Lt[m * NB + l]), zz[l]);
+                  zz[m] = v;
+                }
               }
-              unit_rows(A, za, B, zb, sub, T);
             }
-            __syncthreads();  // zsh is reused by the next chunk
+          };
+          // The rows of a unit as one sequence of virtual rows v = sub, sub+T,
+          // ... < lena + lenb: v < lena is row v of column a, the rest row
+          // v - lena of column b.  A pair unit has M+1 virtual rows and an R
+          // unit M, so the threads of a warp (consecutive units) run the same
+          // trip count and their FP64 instructions keep every lane busy.
+          struct Col {
+            int kind, j, mcol, len;
+            double2* col;
+          };
+          auto unit_rows = [&](const Col& A, const double2* za, const Col& B, const double2* zb, int sub, int T) {
+            const int tot = A.len + B.len;
+            // the starting value of virtual row v and where it goes
+            auto load = [&](int v, int* irow, double2** dst) {
+              const bool inA = v < A.len;
+              const Col& c = inA ? A : B;
+              const int i = inA ? v : v - A.len;
+              *irow = i;
+              *dst = c.col + (int64_t)i * M;
+              if (c.kind == 1) {
+                double2 x = Ub[i * NB + c.mcol];
+                if (i == c.j) x.x += 1.0;
+                return x;
+              }
+              return __ldcg(*dst);
+            };
+            int v = sub;
+            for (; v < tot; v += T) {
+              int i;
+              double2* d;
+              double2 x = load(v, &i, &d);
+              const bool a0 = v < A.len;
+              const double2* ui = Ub + i * NB;
+  #pragma unroll
+              for (int k = 0; k < NB; ++k)
+                if (k < nbk) x = cfms(x, cneg(ui[k]), a0 ? za[k] : zb[k]);
+              *d = x;
+            }
+          };
+          // Which kind of W column j is: 1 if it is pivot mcol of this panel.
+          auto w_kind = [&](int j, int* mcol) {
+            *mcol = -1;
+            if (used[j] && !used0[j]) {
+              for (int m = 0; m < nbk; ++m)
+                if (piv[k0 + m] == j) *mcol = m;
+              return 1;
+            }
+            return 0;
+          };
+          // Units: the W column pairs (q, M-1-q), M+1 rows together, then the
+          // R columns (M rows), dealt round-robin to the cluster's CTAs.  T
+          // threads share a unit's rows (T = 1, 4 or 8, whichever gives the
+          // fewest rows per thread); with T > 1 the unit's z vectors (two for
+          // a pair) come through shared memory, [NT/4][2][NB] at most.
+          const int P = (M + 1) / 2;
+          const int ucta = (P + (gemm_on ? 0 : M) - rank + C - 1) / C;  // R columns only without the product
+          int T = 1;
+          if (a.force_rowsplit == 1 || a.force_rowsplit == 4 || a.force_rowsplit == 8) {
+            T = a.force_rowsplit;  // the autotuner's choice (the same arithmetic per element)
+          } else {
+            int best = ((ucta + NT - 1) / NT) * (M + 1);
+            for (int t = 4; t <= kSymMaxRowSplit; t *= 2) {
+              const int rows = ((ucta + NT / t - 1) / (NT / t)) * ((M + 1 + t - 1) / t);
+              if (rows < best) {
+                best = rows;
+                T = t;
+              }
+            }
           }
+          const int NCH = NT / T;
+          const int cs = tid % NCH, sub = tid / NCH;
+          for (int c0 = 0; c0 < ucta; c0 += NCH) {
+            const int c = c0 + cs;
+            const bool active = c < ucta;
+            const int u = rank + C * c;
+            int ka = 0, kb = 0, ja = 0, jb = 0, ma = -1, mb = -1, lena = 0, lenb = 0;
+            double2* cola = nullptr;
+            double2* colb2 = nullptr;
+            if (active) {
+              if (u < P) {
+                ja = u;
+                jb = M - 1 - u;
+                lena = ja + 1;
+                lenb = (jb != ja) ? jb + 1 : 0;
+                cola = W + ja;
+                colb2 = W + jb;
+                ka = w_kind(ja, &ma);
+                if (lenb) kb = w_kind(jb, &mb);
+              } else {
+                ka = 2;
+                ja = u - P;
+                lena = M;
+                cola = Rg + ja;
+              }
+            }
+            const Col A{ka, ja, ma, lena, cola};
+            const Col B{kb, jb, mb, lenb, colb2 ? colb2 : cola};
+            double2 za[NB], zb[NB];
+  #pragma unroll
+            for (int k = 0; k < NB; ++k) zb[k] = make_double2(0.0, 0.0);
+            if (T == 1) {
+              if (active) {
+                column_z(ka, ja, ma, cola, za);
+                if (lenb) column_z(kb, jb, mb, colb2, zb);
+                unit_rows(A, za, B, zb, 0, 1);
+              }
+            } else {
+              if (active && sub < 2 && (sub == 0 || lenb)) {
+                double2 zz[NB];
+                if (sub == 0) column_z(ka, ja, ma, cola, zz);
+                else column_z(kb, jb, mb, colb2, zz);
+  #pragma unroll
+                for (int k = 0; k < NB; ++k) zsh[(cs * 2 + sub) * NB + k] = zz[k];
+              }
+              __syncthreads();  // z is read before any row of these columns changes
+              if (active) {
+  #pragma unroll
+                for (int k = 0; k < NB; ++k) za[k] = zsh[(cs * 2) * NB + k];
+                if (lenb) {
+  #pragma unroll
+                  for (int k = 0; k < NB; ++k) zb[k] = zsh[(cs * 2 + 1) * NB + k];
+                }
+                unit_rows(A, za, B, zb, sub, T);
+              }
+              __syncthreads();  // zsh is reused by the next chunk
+            }
+          }
+          cluster.sync();
+        }
+      };
+      // A cluster-wide complex product of two Mb x Mb operands on the tensor
+      // cores (rg_ozaki.cuh): exponents reduced over the cluster, digit planes
+      // in the workspace, then CTA tasks (row tile, group of 8 column tiles),
+      // warp w taking column tile 8 group + w.  getA(i, k) and getB(k, j)
+      // read the operands (only in the first two phases, so out may
+      // overwrite them); out(i, j, re, im) stores C_ij.  Ends with a cluster
+      // barrier.
+      auto cluster_zgemm = [&](const int Mb, auto getA, auto getB, auto out) {
+        const int T = oz::tiles(Mb);
+        for (int i = tid; i < 16 * T; i += NT) {
+          ea_s[i] = oz::kNoExp;
+          eb_s[i] = oz::kNoExp;
+        }
+        __syncthreads();
+        for (int64_t e = ctid; e < (int64_t)Mb * Mb; e += CNT) {
+          const int i = (int)(e / Mb), j = (int)(e % Mb);
+          atomicMax(ea_s + i, oz::fexp2(getA(i, j)));
+          atomicMax(eb_s + j, oz::fexp2(getB(i, j)));
+        }
+        __syncthreads();
+        int* mine = expart + rank * 32 * T;
+        for (int i = tid; i < 16 * T; i += NT) {
+          mine[i] = ea_s[i];
+          mine[16 * T + i] = eb_s[i];
+        }
+        cluster.sync();
+        for (int i = tid; i < 16 * T; i += NT) {
+          int x = oz::kNoExp, y = oz::kNoExp;
+          for (int c = 0; c < C; ++c) {
+            x = max(x, __ldcg(expart + c * 32 * T + i));
+            y = max(y, __ldcg(expart + c * 32 * T + 16 * T + i));
+          }
+          ea_s[i] = x;
+          eb_s[i] = y;
+        }
+        __syncthreads();
+        oz::split_a(Mb, getA, ea_s, adig, ctid, CNT);
+        oz::split_b(Mb, getB, eb_s, bdig, ctid, CNT);
+        cluster.sync();  // every digit is written before any CTA reads them
+        const int ngroup = (T + 7) / 8;
+        const int64_t plane = (int64_t)T * T * 32;
+        for (int task = rank; task < T * ngroup; task += C) {
+          const int ti = task / ngroup, tj = (task % ngroup) * 8 + warp;
+          auto stage = [&](int ch) {
+            __syncthreads();  // the previous chunk's digits have been used
+            const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
+            for (int e = tid; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += NT) {
+              const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
+              if (kk < nk)
+                astage[e] = __ldcg(adig + ps * plane + ((int64_t)ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
+            }
+            __syncthreads();
+          };
+          oz::gemm_tile(Mb, ti, tj, tj < T, bdig, ea_s, eb_s, astage, stage, out);
+        }
+        cluster.sync();
+      };
+      auto wsym = [&](const double2* Wb, int Mb, int i, int j) {  // symmetric matrix from its upper triangle
+        return __ldcg(Wb + (i <= j ? (int64_t)i * Mb + j : (int64_t)j * Mb + i));
+      };
+
+      if (!split) {
+        gj(W, M);
+      } else {
+        // X^-1 by its 2 x 2 block form, X = [[A, B], [B^T, D]] with h x h
+        // blocks: two half-size Gauss-Jordan inverses in FP64 (M^3 flops
+        // instead of 4 M^3) and four half-size products on the tensor cores:
+        //   T = A^-1 B,  S = D - B^T T,  Y12 = -T S^-1,  Y11 = A^-1 - Y12 T^T,
+        //   Y22 = S^-1.
+        // A small pivot in either half flags the realization as the full
+        // elimination does.
+        const int h = M >> 1;
+        const int64_t hh = (int64_t)h * h;
+        for (int64_t e = ctid; e < hh; e += CNT) {  // A into Wa (upper triangle)
+          const int i = (int)(e / h), j = (int)(e % h);
+          if (i <= j) Wa[e] = __ldcg(W + (int64_t)i * M + j);
+        }
+        cluster.sync();
+        gj(Wa, h);  // Wa = A^-1
+        cluster_zgemm(
+            h, [&](int i, int k) { return wsym(Wa, h, i, k); },
+            [&](int k, int j) { return __ldcg(W + (int64_t)k * M + h + j); },
+            [&](int i, int j, double re, double im) { Tb[(int64_t)i * h + j] = make_double2(re, im); });
+        cluster_zgemm(
+            h, [&](int i, int k) { return __ldcg(W + (int64_t)k * M + h + i); },
+            [&](int k, int j) { return __ldcg(Tb + (int64_t)k * h + j); },
+            [&](int i, int j, double re, double im) {
+              if (i <= j) {
+                const double2 d = __ldcg(W + (int64_t)(h + i) * M + h + j);
+                Ws[(int64_t)i * h + j] = make_double2(d.x - re, d.y - im);
+              }
+            });
+        gj(Ws, h);  // Ws = S^-1
+        cluster_zgemm(
+            h, [&](int i, int k) { return __ldcg(Tb + (int64_t)i * h + k); },
+            [&](int k, int j) { return wsym(Ws, h, k, j); },
+            [&](int i, int j, double re, double im) { W[(int64_t)i * M + h + j] = make_double2(-re, -im); });
+        cluster_zgemm(
+            h, [&](int i, int k) { return __ldcg(W + (int64_t)i * M + h + k); },
+            [&](int k, int j) { return __ldcg(Tb + (int64_t)j * h + k); },
+            [&](int i, int j, double re, double im) {
+              if (i <= j) {
+                const double2 ai = wsym(Wa, h, i, j);
+                W[(int64_t)i * M + j] = make_double2(ai.x - re, ai.y - im);
+              }
+            });
+        for (int64_t e = ctid; e < hh; e += CNT) {  // Y22 = S^-1
+          const int i = (int)(e / h), j = (int)(e % h);
+          if (i <= j) W[(int64_t)(h + i) * M + h + j] = __ldcg(Ws + e);
         }
         cluster.sync();
       }
+
       if (gemm_on) {
         // 4. B Gs1 <- X^-1 (B Gs1) on the tensor cores (rg_ozaki.cuh).
-        const int T = oz::tiles(M);
         if (n < a.inject_at) {
           // before the source slice the right-hand side is zero and stays zero
         } else if (n == a.inject_at) {
@@ -587,70 +715,16 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           const double sg = n == 0 ? 1.0 : -1.0;
           for (int64_t e = ctid; e < mm; e += CNT) {
             const int i = (int)(e / M), j = (int)(e % M);
-            Rg[e] = cscale(sg, __ldcg(W + (i <= j ? (int64_t)i * M + j : (int64_t)j * M + i)));
+            Rg[e] = cscale(sg, wsym(W, M, i, j));
           }
+          cluster.sync();  // the new right-hand side is complete before the next slice
         } else {
-          // a. exponents of the rows of X^-1 (symmetric: its columns too) and
-          //    of the columns of B Gs1, reduced over the cluster
-          for (int i = tid; i < 16 * T; i += NT) {
-            ea_s[i] = oz::kNoExp;
-            eb_s[i] = oz::kNoExp;
-          }
-          __syncthreads();
-          for (int64_t e = ctid; e < mm; e += CNT) {
-            const int i = (int)(e / M), j = (int)(e % M);
-            if (i <= j) {
-              const int ew = oz::fexp2(__ldcg(W + e));
-              atomicMax(ea_s + i, ew);
-              if (j != i) atomicMax(ea_s + j, ew);
-            }
-            atomicMax(eb_s + j, oz::fexp2(__ldcg(Rg + e)));
-          }
-          __syncthreads();
-          int* mine = expart + rank * 32 * T;
-          for (int i = tid; i < 16 * T; i += NT) {
-            mine[i] = ea_s[i];
-            mine[16 * T + i] = eb_s[i];
-          }
-          cluster.sync();
-          for (int i = tid; i < 16 * T; i += NT) {
-            int x = oz::kNoExp, y = oz::kNoExp;
-            for (int c = 0; c < C; ++c) {
-              x = max(x, __ldcg(expart + c * 32 * T + i));
-              y = max(y, __ldcg(expart + c * 32 * T + 16 * T + i));
-            }
-            ea_s[i] = x;
-            eb_s[i] = y;
-          }
-          __syncthreads();
-          // b. digit planes of both operands (split over the cluster)
-          oz::split_a(
-              M, [&](int i, int k) { return __ldcg(W + (i <= k ? (int64_t)i * M + k : (int64_t)k * M + i)); }, ea_s,
-              adig, ctid, CNT);
-          oz::split_b(M, [&](int k, int j) { return __ldcg(Rg + (int64_t)k * M + j); }, eb_s, bdig, ctid, CNT);
-          cluster.sync();  // every digit is written before any CTA reads them
-          // c. the product: CTA task = (row tile, group of 8 column tiles),
-          //    warp w takes column tile 8 group + w; the result overwrites
-          //    B Gs1 in place (its digits are already taken)
-          const int ngroup = (T + 7) / 8;
-          const int64_t plane = (int64_t)T * T * 32;
-          for (int task = rank; task < T * ngroup; task += C) {
-            const int ti = task / ngroup, tj = (task % ngroup) * 8 + warp;
-            auto stage = [&](int ch) {
-              __syncthreads();  // the previous chunk's digits have been used
-              const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
-              for (int e = tid; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += NT) {
-                const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
-                if (kk < nk)
-                  astage[e] = __ldcg(adig + ps * plane + ((int64_t)ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
-              }
-              __syncthreads();
-            };
-            oz::gemm_tile(M, ti, tj, tj < T, bdig, ea_s, eb_s, astage, stage,
-                          [&](int i, int j, double re, double im) { Rg[(int64_t)i * M + j] = make_double2(re, im); });
-          }
+          // the result overwrites B Gs1 in place (its digits are already taken)
+          cluster_zgemm(
+              M, [&](int i, int k) { return wsym(W, M, i, k); },
+              [&](int k, int j) { return __ldcg(Rg + (int64_t)k * M + j); },
+              [&](int i, int j, double re, double im) { Rg[(int64_t)i * M + j] = make_double2(re, im); });
         }
-        cluster.sync();  // the new right-hand side is complete before the next slice
       }
       if (a.state_dump && *status0 != kStatusNeedPivot) {
         // The state after this slice, natural order: Gss = W (symmetric,
