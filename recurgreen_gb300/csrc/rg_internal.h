@@ -140,6 +140,10 @@ struct SweepArgs {
   // Gauss-Jordan sweeps and four half-size tensor-core products.  Set from
   // RG_SPLIT_INVERSE (default on).
   int split_inverse;
+  // 1: the tensor-core product copies the next digit pair's B digits into
+  // shared memory (cp.async) while the current pair runs; 0: each pair reads
+  // them from L2 when it starts.  Set from RG_B_PREFETCH (default on).
+  int b_prefetch;
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were
@@ -230,6 +234,7 @@ struct GreenView {
   double sym_tau;        // its pivot threshold
   int tensor_r;          // SweepArgs::tensor_r for this guide
   int split_inverse;     // SweepArgs::split_inverse for this guide
+  int b_prefetch;        // SweepArgs::b_prefetch for this guide
 };
 int green_view(const rg_waveguide* w, GreenView* out);
 

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kOzThreads, 2) zb_gemm_kernel(int M, char* ws,
     __syncthreads();
   };
   double2* c = C + (int64_t)item * strideC;
-  oz::gemm_tile(M, ti, tj, tj < T, w.bdig, w.ea, w.eb, astage, stage, [&](int i, int j, double re, double im) {
+  oz::gemm_tile(M, ti, tj, tj < T, w.bdig, w.ea, w.eb, astage, nullptr, stage, [&](int i, int j, double re, double im) {
     double2 v = make_double2(alpha.x * re - alpha.y * im, alpha.x * im + alpha.y * re);
     if (beta != 0.0) {
       const double2 d = zat(D, item, M, i, j);

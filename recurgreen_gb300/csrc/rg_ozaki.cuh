@@ -192,15 +192,29 @@ __device__ __forceinline__ void mma16816(float c[4], const uint4& a, uint32_t b0
       : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
 }
 
+__device__ __forceinline__ void cp_async16(uint4* smem_dst, const uint4* gsrc) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// uint4 of one warp's B prefetch buffer: two slots of [2 parts][kChunkTiles][32 lanes].
+constexpr int kBringUint4 = 2 * 2 * kChunkTiles * 32;
+
 // One warp's 16 x 16 complex tile (ti, tj) of C = A B over all k.  The A
 // digits of the current chunk come from shared memory (astage: [2][8][4][32]
-// uint4, filled by the caller's stage_a for this row tile and chunk); the B
-// digits are read from global memory (L2).  `stage` is called with the chunk
-// index before the chunk's products and must leave astage filled for every
-// warp (it synchronises the CTA).  out(i, j, re, im) stores C_ij.
+// uint4, filled by the caller's stage for this row tile and chunk); the B
+// digits come from global memory (L2).  With bring (this warp's kBringUint4
+// uint4 of shared memory), the B digits of the next digit pair are copied
+// into the other of two slots with cp.async while the current pair's
+// products run, so the L2 latency overlaps the tensor-core work; each lane
+// copies and reads only its own 16-byte elements.  `stage` is called with
+// the chunk index before the chunk's products and must leave astage filled
+// for every warp (it synchronises the CTA).  out(i, j, re, im) stores C_ij.
 template <class Stage, class Out>
 __device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig, const int* ea, const int* eb,
-                          const uint4* astage, Stage stage, Out out) {
+                          const uint4* astage, uint4* bring, Stage stage, Out out) {
   const int T = tiles(M);
   const int lane = threadIdx.x & 31;
   const int64_t bplane = (int64_t)T * T * 32;
@@ -208,6 +222,20 @@ __device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig,
 #pragma unroll
   for (int k = 0; k < 16; ++k) hi[k] = lo[k] = 0;
   const int nchunk = (T + kChunkTiles - 1) / kChunkTiles;
+  // the B digits of (chunk ch, slice q) into slot `slot` of bring
+  auto fetch = [&](int ch, int q, int slot) {
+    const int nk = min(kChunkTiles, T - ch * kChunkTiles);
+    const uint4* src = bdig + ((int64_t)tj * T + ch * kChunkTiles) * 32 + lane;
+    uint4* dst = bring + slot * (2 * kChunkTiles * 32) + lane;
+#pragma unroll
+    for (int part = 0; part < 2; ++part)
+#pragma unroll
+      for (int kk = 0; kk < kChunkTiles; ++kk)
+        if (kk < nk) cp_async16(dst + (part * kChunkTiles + kk) * 32, src + (int64_t)(part * kSlices + q) * bplane + kk * 32);
+    cp_async_commit();
+  };
+  int slot = 0;
+  if (active && bring) fetch(0, 0, 0);
   for (int ch = 0; ch < nchunk; ++ch) {
     stage(ch);
     const int nk = min(kChunkTiles, T - ch * kChunkTiles);
@@ -224,26 +252,43 @@ __device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig,
 #pragma unroll 1
         for (int p = p0; p <= p1; ++p) {
           const int q = l - p;
-          const uint4* br = bbase + (int64_t)q * bplane;
-          const uint4* bi = bbase + (int64_t)(kSlices + q) * bplane;
+          const uint4* cur = nullptr;
+          if (bring) {
+            // this pair's B digits have landed in `slot`; start copying the
+            // next pair's (possibly of the next chunk) into the other slot
+            cp_async_wait_all();
+            cur = bring + slot * (2 * kChunkTiles * 32) + lane;
+            int nl = l, np = p + 1, nch = ch;
+            if (np > p1) {
+              nl = l + 1;
+              if (nl > kLmax) {
+                nl = 0;
+                ++nch;
+              }
+              np = max(0, nl - (kSlices - 1));
+            }
+            if (nch < nchunk) fetch(nch, nl - np, slot ^ 1);
+          }
           const uint4* ar = astage + (p * kChunkTiles) * 32 + lane;
           const uint4* ai = astage + ((kSlices + p) * kChunkTiles) * 32 + lane;
 #pragma unroll
           for (int kk = 0; kk < kChunkTiles; ++kk) {
             if (kk < nk) {
-              const uint4 vbr = __ldcg(br + kk * 32), vbi = __ldcg(bi + kk * 32);
+              const uint4 vb = cur ? cur[kk * 32] : __ldcg(bbase + (int64_t)q * bplane + kk * 32);
+              const uint4 vc = cur ? cur[(kChunkTiles + kk) * 32] : __ldcg(bbase + (int64_t)(kSlices + q) * bplane + kk * 32);
               const uint4 var = ar[kk * 32], vai = ai[kk * 32];
               // re += Ar Br - Ai Bi; im += Ar Bi + Ai Br
-              mma16816(acc[0], var, vbr.x, vbr.y);
-              mma16816(acc[0], vai, vbi.x ^ 0x80008000u, vbi.y ^ 0x80008000u);
-              mma16816(acc[1], var, vbr.z, vbr.w);
-              mma16816(acc[1], vai, vbi.z ^ 0x80008000u, vbi.w ^ 0x80008000u);
-              mma16816(acc[2], var, vbi.x, vbi.y);
-              mma16816(acc[2], vai, vbr.x, vbr.y);
-              mma16816(acc[3], var, vbi.z, vbi.w);
-              mma16816(acc[3], vai, vbr.z, vbr.w);
+              mma16816(acc[0], var, vb.x, vb.y);
+              mma16816(acc[0], vai, vc.x ^ 0x80008000u, vc.y ^ 0x80008000u);
+              mma16816(acc[1], var, vb.z, vb.w);
+              mma16816(acc[1], vai, vc.z ^ 0x80008000u, vc.w ^ 0x80008000u);
+              mma16816(acc[2], var, vc.x, vc.y);
+              mma16816(acc[2], vai, vb.x, vb.y);
+              mma16816(acc[3], var, vc.z, vc.w);
+              mma16816(acc[3], vai, vb.z, vb.w);
             }
           }
+          slot ^= 1;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)

@@ -63,8 +63,8 @@ constexpr int kSplitMinModes = 128;
 // share one region: they are never live at the same time.
 //
 // With tensor_r the product's staged A digits ([2][8][4][32] uint4, 32 KB)
-// overlay the start of this area (dead during the product), and two arrays
-// of 16-padded exponents follow it.
+// and the warps' B prefetch slots (8 x 8 KB) overlay the start of this area
+// (dead during the product), and two arrays of 16-padded exponents follow.
 struct LargeSymSmem {
   __host__ __device__ static size_t shared_region(int M) {
     const size_t z = (size_t)(kSymNT / 4) * 2 * kSymNB;
@@ -74,7 +74,9 @@ struct LargeSymSmem {
     return sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
            sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
   }
-  static constexpr size_t kStage = sizeof(uint4) * 2 * oz::kSlices * oz::kChunkTiles * 32;
+  // the staged A digits, then each warp's B prefetch slots
+  static constexpr size_t kStage =
+      sizeof(uint4) * (2 * oz::kSlices * oz::kChunkTiles * 32 + (kSymNT / 32) * oz::kBringUint4);
   __host__ __device__ static size_t exps_offset(int M) {
     const size_t b = sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
                      sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
@@ -107,6 +109,77 @@ inline int64_t large_sym_stride(int M, int ny, bool tensor) {
 
 __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
 
+// An operand of a cluster product: entry (r, c) is p[r ld + c + off], or,
+// with trans, p[c ld + r + off], or, with sym, the symmetric matrix stored
+// as the upper triangle at p (row stride ld).
+struct Opnd {
+  const double2* p;
+  int64_t ld, off;
+  int sym, trans;
+};
+
+__device__ __forceinline__ double2 opnd_at(const Opnd& o, int r, int c) {
+  if (o.sym) return __ldcg(o.p + (r <= c ? (int64_t)r * o.ld + c : (int64_t)c * o.ld + r));
+  return o.trans ? __ldcg(o.p + (int64_t)c * o.ld + r + o.off) : __ldcg(o.p + (int64_t)r * o.ld + c + o.off);
+}
+
+// Where one output tile of a cluster product goes:
+//   dst[i ld + j + off] = sign C_ij + aux(i, j)   (only i <= j when upper),
+// aux(i, j) = 0, or aux[i aux_ld + j + aux_off], or, with aux_sym, the
+// symmetric matrix stored as the upper triangle at aux (row stride aux_ld).
+struct TileOut {
+  double2* dst;
+  int64_t ld, off;
+  double sign;
+  const double2* aux;
+  int64_t aux_ld, aux_off;
+  int aux_sym, upper;
+};
+
+struct TileJob {
+  int Mb, ti, tj, active;
+  const uint4* adig;
+  const uint4* bdig;
+  const int* ea;
+  const int* eb;
+  uint4* astage;
+  uint4* bring;
+  TileOut o;
+};
+
+// One warp's 16 x 16 tile of a cluster product (every warp of the CTA calls
+// it for the same row tile; the A digits are staged per chunk with two CTA
+// barriers).  Not inlined: one copy of the tensor-core loop, with its own
+// register allocation, serves all of a slice's products.
+__device__ __noinline__ void tile_product(const TileJob jb) {
+  const int T = oz::tiles(jb.Mb);
+  const int64_t plane = (int64_t)T * T * 32;
+  auto stage = [&](int ch) {
+    __syncthreads();  // the previous chunk's digits have been used
+    const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
+    for (int e = threadIdx.x; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += blockDim.x) {
+      const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
+      if (kk < nk)
+        jb.astage[e] = __ldcg(jb.adig + ps * plane + ((int64_t)jb.ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
+    }
+    __syncthreads();
+  };
+  const TileOut& o = jb.o;
+  oz::gemm_tile(jb.Mb, jb.ti, jb.tj, jb.active != 0, jb.bdig, jb.ea, jb.eb, jb.astage, jb.bring, stage,
+                [&](int i, int j, double re, double im) {
+                  if (o.upper && i > j) return;
+                  double2 v = make_double2(o.sign * re, o.sign * im);
+                  if (o.aux) {
+                    const double2 x = o.aux_sym ? __ldcg(o.aux + (i <= j ? (int64_t)i * o.aux_ld + j
+                                                                           : (int64_t)j * o.aux_ld + i))
+                                                : __ldcg(o.aux + (int64_t)i * o.aux_ld + j + o.aux_off);
+                    v.x += x.x;
+                    v.y += x.y;
+                  }
+                  o.dst[(int64_t)i * o.ld + j + o.off] = v;
+                });
+}
+
 __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a) {
   constexpr int NT = kSymNT, NB = kSymNB, NW = NT / 32;
   cg::cluster_group cluster = cg::this_cluster();
@@ -137,6 +210,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
   // the propagator product on the tensor cores
   const bool gemm_on = a.tensor_r != 0;
   uint4* astage = reinterpret_cast<uint4*>(sm);  // overlays the panel arrays during the product
+  uint4* bring = astage + 2 * oz::kSlices * oz::kChunkTiles * 32 + (threadIdx.x >> 5) * oz::kBringUint4;
   int* ea_s = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + LargeSymSmem::exps_offset(MX));
   int* eb_s = ea_s + 16 * oz::tiles(MX);
 
@@ -597,9 +671,10 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
       // in the workspace, then CTA tasks (row tile, group of 8 column tiles),
       // warp w taking column tile 8 group + w.  getA(i, k) and getB(k, j)
       // read the operands (only in the first two phases, so out may
-      // overwrite them); out(i, j, re, im) stores C_ij.  Ends with a cluster
-      // barrier.
-      auto cluster_zgemm = [&](const int Mb, auto getA, auto getB, auto out) {
+      // overwrite them); out says where C goes.  Ends with a cluster barrier.
+      auto cluster_zgemm = [&](const int Mb, const Opnd& A, const Opnd& B, const TileOut& out) {
+        auto getA = [&](int i, int k) { return opnd_at(A, i, k); };
+        auto getB = [&](int k, int j) { return opnd_at(B, k, j); };
         const int T = oz::tiles(Mb);
         for (int i = tid; i < 16 * T; i += NT) {
           ea_s[i] = oz::kNoExp;
@@ -632,20 +707,10 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
         oz::split_b(Mb, getB, eb_s, bdig, ctid, CNT);
         cluster.sync();  // every digit is written before any CTA reads them
         const int ngroup = (T + 7) / 8;
-        const int64_t plane = (int64_t)T * T * 32;
         for (int task = rank; task < T * ngroup; task += C) {
           const int ti = task / ngroup, tj = (task % ngroup) * 8 + warp;
-          auto stage = [&](int ch) {
-            __syncthreads();  // the previous chunk's digits have been used
-            const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
-            for (int e = tid; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += NT) {
-              const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
-              if (kk < nk)
-                astage[e] = __ldcg(adig + ps * plane + ((int64_t)ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
-            }
-            __syncthreads();
-          };
-          oz::gemm_tile(Mb, ti, tj, tj < T, bdig, ea_s, eb_s, astage, stage, out);
+          tile_product(TileJob{Mb, ti, tj, tj < T ? 1 : 0, adig, bdig, ea_s, eb_s, astage,
+                               a.b_prefetch ? bring : nullptr, out});
         }
         cluster.sync();
       };
@@ -671,33 +736,12 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
         }
         cluster.sync();
         gj(Wa, h);  // Wa = A^-1
-        cluster_zgemm(
-            h, [&](int i, int k) { return wsym(Wa, h, i, k); },
-            [&](int k, int j) { return __ldcg(W + (int64_t)k * M + h + j); },
-            [&](int i, int j, double re, double im) { Tb[(int64_t)i * h + j] = make_double2(re, im); });
-        cluster_zgemm(
-            h, [&](int i, int k) { return __ldcg(W + (int64_t)k * M + h + i); },
-            [&](int k, int j) { return __ldcg(Tb + (int64_t)k * h + j); },
-            [&](int i, int j, double re, double im) {
-              if (i <= j) {
-                const double2 d = __ldcg(W + (int64_t)(h + i) * M + h + j);
-                Ws[(int64_t)i * h + j] = make_double2(d.x - re, d.y - im);
-              }
-            });
+        cluster_zgemm(h, Opnd{Wa, h, 0, 1, 0}, Opnd{W, M, h, 0, 0}, TileOut{Tb, h, 0, 1.0, nullptr, 0, 0, 0, 0});
+        cluster_zgemm(h, Opnd{W, M, h, 0, 1}, Opnd{Tb, h, 0, 0, 0},
+                      TileOut{Ws, h, 0, -1.0, W, M, (int64_t)h * M + h, 0, 1});
         gj(Ws, h);  // Ws = S^-1
-        cluster_zgemm(
-            h, [&](int i, int k) { return __ldcg(Tb + (int64_t)i * h + k); },
-            [&](int k, int j) { return wsym(Ws, h, k, j); },
-            [&](int i, int j, double re, double im) { W[(int64_t)i * M + h + j] = make_double2(-re, -im); });
-        cluster_zgemm(
-            h, [&](int i, int k) { return __ldcg(W + (int64_t)i * M + h + k); },
-            [&](int k, int j) { return __ldcg(Tb + (int64_t)j * h + k); },
-            [&](int i, int j, double re, double im) {
-              if (i <= j) {
-                const double2 ai = wsym(Wa, h, i, j);
-                W[(int64_t)i * M + j] = make_double2(ai.x - re, ai.y - im);
-              }
-            });
+        cluster_zgemm(h, Opnd{Tb, h, 0, 0, 0}, Opnd{Ws, h, 0, 1, 0}, TileOut{W, M, h, -1.0, nullptr, 0, 0, 0, 0});
+        cluster_zgemm(h, Opnd{W, M, h, 0, 0}, Opnd{Tb, h, 0, 0, 1}, TileOut{W, M, 0, -1.0, Wa, h, 0, 1, 1});
         for (int64_t e = ctid; e < hh; e += CNT) {  // Y22 = S^-1
           const int i = (int)(e / h), j = (int)(e % h);
           if (i <= j) W[(int64_t)(h + i) * M + h + j] = __ldcg(Ws + e);
@@ -720,10 +764,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           cluster.sync();  // the new right-hand side is complete before the next slice
         } else {
           // the result overwrites B Gs1 in place (its digits are already taken)
-          cluster_zgemm(
-              M, [&](int i, int k) { return wsym(W, M, i, k); },
-              [&](int k, int j) { return __ldcg(Rg + (int64_t)k * M + j); },
-              [&](int i, int j, double re, double im) { Rg[(int64_t)i * M + j] = make_double2(re, im); });
+          cluster_zgemm(M, Opnd{W, M, 0, 1, 0}, Opnd{Rg, M, 0, 0, 0}, TileOut{Rg, M, 0, 1.0, nullptr, 0, 0, 0, 0});
         }
       }
       if (a.state_dump && *status0 != kStatusNeedPivot) {

@@ -28,7 +28,10 @@ Configurations:
            L1 = Tr(t^H t) and L2 = Tr((t^H t)^2) from the oracle, for the
            adjoint gradient test, at the step 1e-6 sigma_U and, as a reference
            with less rounding noise, Richardson-extrapolated from the steps
-           16e-6 and 32e-6 sigma_U: (4 D(h) - D(2h)) / 3 cancels the h^2 term.
+           64e-6 and 128e-6 sigma_U: (4 D(h) - D(2h)) / 3 cancels the h^2 term
+           (the oracle's rounding noise in D falls as 1/h: ~1e-5 of the
+           largest value at 1e-6 sigma_U, ~2e-7 at 64e-6 sigma_U; the h^4
+           term left is below 1e-7).
 
 Usage:  python tests/golden/make_large_fixtures.py c5short [--threads 2]
         python tests/golden/make_large_fixtures.py c5 [--threads 8]
@@ -135,8 +138,8 @@ def make_diff(threads: int) -> None:
 
     def one(job):
         s, c, ix, iy = job
-        d1, d16, d32 = (central(s, ix, iy, m * h) for m in (1, 16, 32))
-        return s, c, d1, (4 * d16 - d32) / 3
+        d1, d64, d128 = (central(s, ix, iy, m * h) for m in (1, 64, 128))
+        return s, c, d1, (4 * d64 - d128) / 3
 
     t0 = time.time()
     with ThreadPoolExecutor(max_workers=threads) as ex:

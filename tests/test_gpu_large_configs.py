@@ -185,8 +185,8 @@ def test_adjoint_fd_at_differentiation_config():
     At the step 1e-6 sigma_U the differences carry the oracle's FP64 rounding
     noise over 1000 slices, a few 1e-6 of the largest sampled value (it shows
     as the spread between steps); the reference of record is therefore the
-    Richardson extrapolation of the steps 16e-6 and 32e-6 sigma_U, whose noise
-    is ~20x smaller: the adjoint must match it within 1e-6 of its largest
+    Richardson extrapolation of the steps 64e-6 and 128e-6 sigma_U, whose noise
+    is ~40x smaller: the adjoint must match it within 1e-6 of its largest
     value, and the 1e-6-step differences within their own measured deviation
     from it plus 1e-6.  The losses match the oracle's within 1e-10."""
     torch = pytest.importorskip("torch")
