@@ -107,24 +107,30 @@ def executed_flops(M: int, nx: int, kernel: str) -> tuple[float, float]:
     """(FP64 flops, FP16 tensor flops) the sweep executes for one realization:
       * shared-memory symmetric kernel (M <= 64): 12 M^3 + 4 M^2 FP64 per slice;
       * blocked symmetric kernel with the tensor-core propagator product
-        (64 < M <= 512): the inverse in FP64 -- 4 M^3, or M^3 in its 2 x 2
-        block form (even M >= 128) -- and 43 digit pairs x 4 real products
-        x 2 k^3 FP16 flops per k x k product: 344 M^3 for the propagator
-        product plus 4 x 344 (M/2)^3 for the block form's products;
+        (64 < M <= 512): the inverse in FP64 -- 4 M^3 for one Gauss-Jordan
+        sweep; each level of the 2 x 2 block form (even sizes >= 128, at most
+        two levels) replaces a size-m inverse by two of size m/2 and four
+        (m/2)^3 products -- and 43 digit pairs x 4 real products x 2 k^3 FP16
+        flops per k x k product: 344 M^3 for the propagator product plus
+        4 x 344 (m/2)^3 per block split;
       * otherwise the pivoted reference count 16 M^3 in FP64.
-    RG_TENSOR_R=0 / RG_SPLIT_INVERSE=0 select the FP64-only variants."""
+    RG_TENSOR_R=0 / RG_SPLIT_INVERSE=0 or 1 select the other variants."""
     tensor = os.environ.get("RG_TENSOR_R", "1") != "0" and 64 < M <= 512
-    split = tensor and os.environ.get("RG_SPLIT_INVERSE", "1") != "0" and M >= 128 and M % 2 == 0
+    want = {"0": 0, "1": 1}.get(os.environ.get("RG_SPLIT_INVERSE", "2"), 2)
     if kernel == "symmetric":
         return flops_symmetric(M, nx), 0.0
     if kernel != "blocked_symmetric":
         return flops_per_realization(M, nx), 0.0
     if not tensor:
         return flops_symmetric(M, nx), 0.0
-    h = M // 2
-    fp64 = (2 * 4.0 * h ** 3 if split else 4.0 * M ** 3) * nx
-    fp16 = (344.0 * M ** 3 + (4 * 344.0 * h ** 3 if split else 0.0)) * nx
-    return fp64, fp16
+    fp16 = 344.0 * M ** 3
+    m, blocks = M, 1
+    while want > 0 and m >= 128 and m % 2 == 0:
+        want -= 1
+        fp16 += blocks * 4 * 344.0 * (m // 2) ** 3
+        m, blocks = m // 2, blocks * 2
+    fp64 = blocks * 4.0 * m ** 3
+    return fp64 * nx, fp16 * nx
 
 
 def flops_symmetric(M: int, nx: int) -> float:

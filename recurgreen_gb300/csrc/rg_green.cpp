@@ -140,7 +140,6 @@ int plan_sweep(const GreenView& v, int nk, int source, Arena& ar, DumpSweep* ds,
     ds->sym.sym_tau = v.sym_tau;
     ds->sym.tensor_r = v.tensor_r;
     ds->sym.split_inverse = v.split_inverse;
-    ds->sym.b_prefetch = v.b_prefetch;
     rc = ds->sym_blocked ? rg::sweep_large_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym)
                          : rg::sweep_sym_plan(ds->sym, v.sm_count, &ds->grid_sym, &stride_sym);
     if (rc) return rc;

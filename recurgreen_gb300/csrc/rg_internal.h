@@ -135,15 +135,12 @@ struct SweepArgs {
   // of carrying B Gs1 through the Gauss-Jordan sweep (up to 512 modes).
   // Set from RG_TENSOR_R (default on).
   int tensor_r;
-  // 1 (with tensor_r): above 127 modes, even mode counts, the blocked
-  // symmetric kernel inverts X in its 2 x 2 block form, two half-size FP64
-  // Gauss-Jordan sweeps and four half-size tensor-core products.  Set from
-  // RG_SPLIT_INVERSE (default on).
+  // With tensor_r, the levels (0..2) of the 2 x 2 block inverse of X in the
+  // blocked symmetric kernel: each level halves an even size of at least 128
+  // modes into two half-size inverses and four half-size tensor-core
+  // products; the blocks left are inverted by FP64 Gauss-Jordan sweeps.
+  // Set from RG_SPLIT_INVERSE (default 2).
   int split_inverse;
-  // 1: the tensor-core product copies the next digit pair's B digits into
-  // shared memory (cp.async) while the current pair runs; 0: each pair reads
-  // them from L2 when it starts.  Set from RG_B_PREFETCH (default on).
-  int b_prefetch;
 };
 
 // Status the symmetric kernel leaves on an item whose diagonal pivots were
@@ -234,7 +231,6 @@ struct GreenView {
   double sym_tau;        // its pivot threshold
   int tensor_r;          // SweepArgs::tensor_r for this guide
   int split_inverse;     // SweepArgs::split_inverse for this guide
-  int b_prefetch;        // SweepArgs::b_prefetch for this guide
 };
 int green_view(const rg_waveguide* w, GreenView* out);
 

@@ -318,5 +318,112 @@ __device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig,
     }
 }
 
+// ---------------------------------------------------------------------------
+// The CTA-blocked product: a CTA of 8 warps computes a 2 x 4 block of 16 x 16
+// complex tiles (warp w: row tile ti0 + w/4, column tile tj0 + w%4).  Per
+// chunk of kBlkChunk k tiles, both operands' digits for the block -- A for 2
+// row tiles, B for 4 column tiles -- are staged in shared memory (stage:
+// kBlkStageUint4 uint4 = 96 KB), so the tensor-core loop reads no global
+// memory; every staged A digit serves 4 tiles and every B digit 2, against
+// 8 and 1 in gemm_tile.  Chunks of 32 complex k keep each level sum below
+// 8 pairs x 64 real products x 127^2 < 2^24.  With `upper`, warps whose tile
+// lies wholly below the diagonal (ti > tj) skip the products (their outputs
+// are not wanted).  out(i, j, re, im) as in gemm_tile.
+// ---------------------------------------------------------------------------
+constexpr int kBlkChunk = 2;
+constexpr int kBlkRows = 2, kBlkCols = 4;
+constexpr int kBlkAUint4 = kBlkRows * 2 * kSlices * kBlkChunk * 32;
+constexpr int kBlkStageUint4 = (kBlkRows + kBlkCols) * 2 * kSlices * kBlkChunk * 32;
+
+template <class Out>
+__device__ void gemm_block(int M, int ti0, int tj0, bool upper, const uint4* adig, const uint4* bdig, const int* ea,
+                           const int* eb, uint4* stg, Out out) {
+  const int T = tiles(M);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wr = warp / kBlkCols, wc = warp % kBlkCols;
+  const int ti = ti0 + wr, tj = tj0 + wc;
+  const bool active = ti < T && tj < T && !(upper && ti > tj);
+  const int64_t plane = (int64_t)T * T * 32;
+  uint4* As = stg;
+  uint4* Bs = stg + kBlkAUint4;
+  long long hi[16], lo[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) hi[k] = lo[k] = 0;
+  const int nchunk = (T + kBlkChunk - 1) / kBlkChunk;
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const int nk = min(kBlkChunk, T - ch * kBlkChunk);
+    __syncthreads();  // the previous chunk's digits have been used
+    // stage index ((tile * 2 + part) * kSlices + slice) * kBlkChunk + kk, then lane
+    for (int e = tid; e < kBlkStageUint4; e += blockDim.x) {
+      const int isB = e >= kBlkAUint4;
+      const int f = isB ? e - kBlkAUint4 : e;
+      const int ln = f & 31, kk = (f >> 5) % kBlkChunk, ps = ((f >> 5) / kBlkChunk) % (2 * kSlices);
+      const int tile = ((f >> 5) / kBlkChunk) / (2 * kSlices);
+      const int t = isB ? tj0 + tile : ti0 + tile;
+      if (t < T && kk < nk)
+        cp_async16(stg + e, (isB ? bdig : adig) + ps * plane + ((int64_t)t * T + ch * kBlkChunk + kk) * 32 + ln);
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    if (active) {
+      const uint4* Aw = As + (wr * 2 * kSlices) * kBlkChunk * 32 + lane;
+      const uint4* Bw = Bs + (wc * 2 * kSlices) * kBlkChunk * 32 + lane;
+#pragma unroll 1
+      for (int l = 0; l <= kLmax; ++l) {
+        float acc[4][4];  // [re n0, re n1, im n0, im n1][4]
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) acc[u][w] = 0.0f;
+        const int p0 = max(0, l - (kSlices - 1)), p1 = min(l, kSlices - 1);
+#pragma unroll 1
+        for (int p = p0; p <= p1; ++p) {
+          const int q = l - p;
+#pragma unroll
+          for (int kk = 0; kk < kBlkChunk; ++kk) {
+            if (kk < nk) {
+              const uint4 var = Aw[(p * kBlkChunk + kk) * 32], vai = Aw[((kSlices + p) * kBlkChunk + kk) * 32];
+              const uint4 vb = Bw[(q * kBlkChunk + kk) * 32], vc = Bw[((kSlices + q) * kBlkChunk + kk) * 32];
+              // re += Ar Br - Ai Bi; im += Ar Bi + Ai Br
+              mma16816(acc[0], var, vb.x, vb.y);
+              mma16816(acc[0], vai, vc.x ^ 0x80008000u, vc.y ^ 0x80008000u);
+              mma16816(acc[1], var, vb.z, vb.w);
+              mma16816(acc[1], vai, vc.z ^ 0x80008000u, vc.w ^ 0x80008000u);
+              mma16816(acc[2], var, vc.x, vc.y);
+              mma16816(acc[2], vai, vb.x, vb.y);
+              mma16816(acc[3], var, vc.z, vc.w);
+              mma16816(acc[3], vai, vb.z, vb.w);
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            const long long v = (long long)__float2int_rn(acc[u][w]);
+            if (l <= 3) hi[u * 4 + w] += v << (7 * (3 - l));
+            else lo[u * 4 + w] += v << (7 * (8 - l));
+          }
+      }
+    }
+  }
+  if (!active) return;
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int i = ti * 16 + g + ((w & 2) ? 8 : 0);
+      const int j = tj * 16 + n * 8 + 2 * t + (w & 1);
+      if (i < M && j < M) {
+        const int e = ea[i] + eb[j];
+        const double re = fma((double)hi[n * 4 + w], 0x1p-35, (double)lo[n * 4 + w] * 0x1p-70);
+        const double im = fma((double)hi[8 + n * 4 + w], 0x1p-35, (double)lo[8 + n * 4 + w] * 0x1p-70);
+        out(i, j, scalbn(re, e), scalbn(im, e));
+      }
+    }
+}
+
 }  // namespace oz
 }  // namespace rg

@@ -74,9 +74,8 @@ struct LargeSymSmem {
     return sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
            sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
   }
-  // the staged A digits, then each warp's B prefetch slots
-  static constexpr size_t kStage =
-      sizeof(uint4) * (2 * oz::kSlices * oz::kChunkTiles * 32 + (kSymNT / 32) * oz::kBringUint4);
+  // both operands' staged digits of a CTA's block of output tiles
+  static constexpr size_t kStage = sizeof(uint4) * oz::kBlkStageUint4;
   __host__ __device__ static size_t exps_offset(int M) {
     const size_t b = sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
                      sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
@@ -104,8 +103,39 @@ __host__ __device__ inline int64_t large_sym_schur_offset(int M, int ny) {
 }
 inline int64_t large_sym_stride(int M, int ny, bool tensor) {
   if (!tensor) return large_sym_base_stride(M, ny);
-  return (large_sym_schur_offset(M, ny) + 3 * (int64_t)(M / 2) * (M / 2) + 15) & ~(int64_t)15;
+  return (large_sym_schur_offset(M, ny) + 3 * (int64_t)(M / 2) * (M / 2) + 3 * (int64_t)(M / 4) * (M / 4) + 15) &
+         ~(int64_t)15;
 }
+
+// Levels of the 2 x 2 block inverse for M modes, at most `want`: a level
+// halves an even size of at least kSplitMinModes.
+__host__ __device__ inline int split_depth(int want, int M) {
+  int d = 0;
+  while (d < want && d < 2 && M >= kSplitMinModes && (M % 2) == 0) {
+    ++d;
+    M >>= 1;
+  }
+  return d;
+}
+
+// The steps of the symmetric inverse for 0, 1 and 2 block levels: code =
+// op * 4 + frame (frame 0: X itself; 1: the block A^-1 of frame 0; 2: its
+// block S).
+enum : int { kInvGJ, kInvCopyA, kInvGJA, kInvT, kInvS, kInvGJS, kInvY12, kInvY11, kInvY22 };
+#define RG_INV(op, f) (unsigned char)((op) * 4 + (f))
+__constant__ unsigned char kInvSteps[3][22] = {
+    {RG_INV(kInvGJ, 0)},
+    {RG_INV(kInvCopyA, 0), RG_INV(kInvGJA, 0), RG_INV(kInvT, 0), RG_INV(kInvS, 0), RG_INV(kInvGJS, 0),
+     RG_INV(kInvY12, 0), RG_INV(kInvY11, 0), RG_INV(kInvY22, 0)},
+    {RG_INV(kInvCopyA, 0),
+     RG_INV(kInvCopyA, 1), RG_INV(kInvGJA, 1), RG_INV(kInvT, 1), RG_INV(kInvS, 1), RG_INV(kInvGJS, 1),
+     RG_INV(kInvY12, 1), RG_INV(kInvY11, 1), RG_INV(kInvY22, 1),
+     RG_INV(kInvT, 0), RG_INV(kInvS, 0),
+     RG_INV(kInvCopyA, 2), RG_INV(kInvGJA, 2), RG_INV(kInvT, 2), RG_INV(kInvS, 2), RG_INV(kInvGJS, 2),
+     RG_INV(kInvY12, 2), RG_INV(kInvY11, 2), RG_INV(kInvY22, 2),
+     RG_INV(kInvY12, 0), RG_INV(kInvY11, 0), RG_INV(kInvY22, 0)}};
+#undef RG_INV
+__constant__ int kInvStepCount[3] = {1, 8, 22};
 
 __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
 
@@ -136,48 +166,104 @@ struct TileOut {
   int aux_sym, upper;
 };
 
-struct TileJob {
-  int Mb, ti, tj, active;
+struct BlockJob {
+  int Mb, ti0, tj0;
   const uint4* adig;
   const uint4* bdig;
   const int* ea;
   const int* eb;
-  uint4* astage;
-  uint4* bring;
+  uint4* stage;
   TileOut o;
 };
 
-// One warp's 16 x 16 tile of a cluster product (every warp of the CTA calls
-// it for the same row tile; the A digits are staged per chunk with two CTA
-// barriers).  Not inlined: one copy of the tensor-core loop, with its own
-// register allocation, serves all of a slice's products.
-__device__ __noinline__ void tile_product(const TileJob jb) {
-  const int T = oz::tiles(jb.Mb);
-  const int64_t plane = (int64_t)T * T * 32;
-  auto stage = [&](int ch) {
-    __syncthreads();  // the previous chunk's digits have been used
-    const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
-    for (int e = threadIdx.x; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += blockDim.x) {
-      const int ln = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
-      if (kk < nk)
-        jb.astage[e] = __ldcg(jb.adig + ps * plane + ((int64_t)jb.ti * T + ch * oz::kChunkTiles + kk) * 32 + ln);
-    }
-    __syncthreads();
-  };
+// One CTA's 2 x 4 block of 16 x 16 output tiles of a cluster product (warp
+// w: row tile ti0 + w/4, column tile tj0 + w%4; both operands' digits staged
+// in shared memory per chunk).  Not inlined: one copy of the tensor-core
+// loop, with its own register allocation, serves all of a slice's products.
+__device__ __noinline__ void block_product(const BlockJob jb) {
   const TileOut& o = jb.o;
-  oz::gemm_tile(jb.Mb, jb.ti, jb.tj, jb.active != 0, jb.bdig, jb.ea, jb.eb, jb.astage, jb.bring, stage,
-                [&](int i, int j, double re, double im) {
-                  if (o.upper && i > j) return;
-                  double2 v = make_double2(o.sign * re, o.sign * im);
-                  if (o.aux) {
-                    const double2 x = o.aux_sym ? __ldcg(o.aux + (i <= j ? (int64_t)i * o.aux_ld + j
-                                                                           : (int64_t)j * o.aux_ld + i))
-                                                : __ldcg(o.aux + (int64_t)i * o.aux_ld + j + o.aux_off);
-                    v.x += x.x;
-                    v.y += x.y;
-                  }
-                  o.dst[(int64_t)i * o.ld + j + o.off] = v;
-                });
+  oz::gemm_block(jb.Mb, jb.ti0, jb.tj0, o.upper != 0, jb.adig, jb.bdig, jb.ea, jb.eb, jb.stage,
+                 [&](int i, int j, double re, double im) {
+                   if (o.upper && i > j) return;
+                   double2 v = make_double2(o.sign * re, o.sign * im);
+                   if (o.aux) {
+                     const double2 x = o.aux_sym ? __ldcg(o.aux + (i <= j ? (int64_t)i * o.aux_ld + j
+                                                                            : (int64_t)j * o.aux_ld + i))
+                                                 : __ldcg(o.aux + (int64_t)i * o.aux_ld + j + o.aux_off);
+                     v.x += x.x;
+                     v.y += x.y;
+                   }
+                   o.dst[(int64_t)i * o.ld + j + o.off] = v;
+                 });
+}
+
+// Where a cluster product keeps its state: the CTA's exponent arrays in
+// shared memory, the cluster's partial exponents and both operands' digit
+// planes in the workspace, and the CTA's staging area.
+struct ZgemmCtx {
+  int* ea_s;
+  int* eb_s;
+  int* expart;
+  uint4* adig;
+  uint4* bdig;
+  uint4* stage;
+};
+
+// A cluster-wide complex product C = A B of two Mb x Mb operands on the
+// tensor cores (rg_ozaki.cuh): exponents reduced over the cluster, digit
+// planes in the workspace, then CTA tasks (blocks of 2 x 4 output tiles,
+// both operands' digits staged in shared memory; with out.upper, blocks
+// wholly below the diagonal are skipped).  The operands are read only in
+// the first two phases, so out may overwrite them.  Called by every thread
+// of the cluster; ends with a cluster barrier.  Not inlined: the slice's
+// five products share one copy.
+__device__ __noinline__ void cluster_zgemm(const ZgemmCtx c, const int Mb, const Opnd A, const Opnd B,
+                                           const TileOut out) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, ctid = rank * kSymNT + tid, CNT = C * kSymNT;
+  auto getA = [&](int i, int k) { return opnd_at(A, i, k); };
+  auto getB = [&](int k, int j) { return opnd_at(B, k, j); };
+  const int T = oz::tiles(Mb);
+  for (int i = tid; i < 16 * T; i += kSymNT) {
+    c.ea_s[i] = oz::kNoExp;
+    c.eb_s[i] = oz::kNoExp;
+  }
+  __syncthreads();
+  for (int64_t e = ctid; e < (int64_t)Mb * Mb; e += CNT) {
+    const int i = (int)(e / Mb), j = (int)(e % Mb);
+    atomicMax(c.ea_s + i, oz::fexp2(getA(i, j)));
+    atomicMax(c.eb_s + j, oz::fexp2(getB(i, j)));
+  }
+  __syncthreads();
+  int* mine = c.expart + rank * 32 * T;
+  for (int i = tid; i < 16 * T; i += kSymNT) {
+    mine[i] = c.ea_s[i];
+    mine[16 * T + i] = c.eb_s[i];
+  }
+  cluster.sync();
+  for (int i = tid; i < 16 * T; i += kSymNT) {
+    int x = oz::kNoExp, y = oz::kNoExp;
+    for (int r = 0; r < C; ++r) {
+      x = max(x, __ldcg(c.expart + r * 32 * T + i));
+      y = max(y, __ldcg(c.expart + r * 32 * T + 16 * T + i));
+    }
+    c.ea_s[i] = x;
+    c.eb_s[i] = y;
+  }
+  __syncthreads();
+  oz::split_a(Mb, getA, c.ea_s, c.adig, ctid, CNT);
+  oz::split_b(Mb, getB, c.eb_s, c.bdig, ctid, CNT);
+  cluster.sync();  // every digit is written before any CTA reads them
+  const int nbr = (T + oz::kBlkRows - 1) / oz::kBlkRows, nbc = (T + oz::kBlkCols - 1) / oz::kBlkCols;
+  int k = 0;
+  for (int bi = 0; bi < nbr; ++bi)
+    for (int bj = 0; bj < nbc; ++bj) {
+      const int ti0 = bi * oz::kBlkRows, tj0 = bj * oz::kBlkCols;
+      if (out.upper && ti0 > tj0 + oz::kBlkCols - 1) continue;
+      if (k++ % C == rank) block_product(BlockJob{Mb, ti0, tj0, c.adig, c.bdig, c.ea_s, c.eb_s, c.stage, out});
+    }
+  cluster.sync();
 }
 
 __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a) {
@@ -209,8 +295,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
   const bool refl = (a.mode == kModeRefl);
   // the propagator product on the tensor cores
   const bool gemm_on = a.tensor_r != 0;
-  uint4* astage = reinterpret_cast<uint4*>(sm);  // overlays the panel arrays during the product
-  uint4* bring = astage + 2 * oz::kSlices * oz::kChunkTiles * 32 + (threadIdx.x >> 5) * oz::kBringUint4;
+  uint4* stage = reinterpret_cast<uint4*>(sm);  // overlays the panel arrays during the product
   int* ea_s = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + LargeSymSmem::exps_offset(MX));
   int* eb_s = ea_s + 16 * oz::tiles(MX);
 
@@ -282,11 +367,16 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
     uint4* adig = reinterpret_cast<uint4*>(ws + large_sym_base_stride(M, ny));  // product digit planes
     uint4* bdig = adig + oz::operand_uint4(M);
     int* expart = reinterpret_cast<int*>(bdig + oz::operand_uint4(M));  // [C][2][16 T] partial exponents
-    // the 2 x 2 block inverse's buffers: A^-1, T = A^-1 B, S^-1 (h x h each)
-    const bool split = gemm_on && a.split_inverse && M >= kSplitMinModes && (M % 2) == 0;
+    // the 2 x 2 block inverse's levels (0: one Gauss-Jordan elimination) and
+    // buffers: A^-1, T = A^-1 B, S^-1 (h x h each, h = M / 2), then the same
+    // for the half-size blocks (M / 4 each)
+    const int split_levels = split_depth(gemm_on ? a.split_inverse : 0, M);
     double2* Wa = ws + large_sym_schur_offset(M, ny);
     double2* Tb = Wa + (int64_t)(M / 2) * (M / 2);
     double2* Ws = Tb + (int64_t)(M / 2) * (M / 2);
+    double2* Wa2 = Ws + (int64_t)(M / 2) * (M / 2);
+    double2* Tb2 = Wa2 + (int64_t)(M / 4) * (M / 4);
+    double2* Ws2 = Tb2 + (int64_t)(M / 4) * (M / 4);
     if (tid == 0) s_status = wd.periodic ? kStatusNeedPivot : RG_OK;  // periodic X is Hermitian, not symmetric
     const double one = a.inject_at > 0 ? 0.0 : 1.0;  // the source at slice 0, or zero until inject_at
     for (int64_t e = ctid; e < mm; e += CNT) Rg[e] = make_double2((e / M) == (e % M) ? one : 0.0, 0.0);
@@ -666,87 +756,59 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           cluster.sync();
         }
       };
-      // A cluster-wide complex product of two Mb x Mb operands on the tensor
-      // cores (rg_ozaki.cuh): exponents reduced over the cluster, digit planes
-      // in the workspace, then CTA tasks (row tile, group of 8 column tiles),
-      // warp w taking column tile 8 group + w.  getA(i, k) and getB(k, j)
-      // read the operands (only in the first two phases, so out may
-      // overwrite them); out says where C goes.  Ends with a cluster barrier.
-      auto cluster_zgemm = [&](const int Mb, const Opnd& A, const Opnd& B, const TileOut& out) {
-        auto getA = [&](int i, int k) { return opnd_at(A, i, k); };
-        auto getB = [&](int k, int j) { return opnd_at(B, k, j); };
-        const int T = oz::tiles(Mb);
-        for (int i = tid; i < 16 * T; i += NT) {
-          ea_s[i] = oz::kNoExp;
-          eb_s[i] = oz::kNoExp;
-        }
-        __syncthreads();
-        for (int64_t e = ctid; e < (int64_t)Mb * Mb; e += CNT) {
-          const int i = (int)(e / Mb), j = (int)(e % Mb);
-          atomicMax(ea_s + i, oz::fexp2(getA(i, j)));
-          atomicMax(eb_s + j, oz::fexp2(getB(i, j)));
-        }
-        __syncthreads();
-        int* mine = expart + rank * 32 * T;
-        for (int i = tid; i < 16 * T; i += NT) {
-          mine[i] = ea_s[i];
-          mine[16 * T + i] = eb_s[i];
-        }
-        cluster.sync();
-        for (int i = tid; i < 16 * T; i += NT) {
-          int x = oz::kNoExp, y = oz::kNoExp;
-          for (int c = 0; c < C; ++c) {
-            x = max(x, __ldcg(expart + c * 32 * T + i));
-            y = max(y, __ldcg(expart + c * 32 * T + 16 * T + i));
-          }
-          ea_s[i] = x;
-          eb_s[i] = y;
-        }
-        __syncthreads();
-        oz::split_a(Mb, getA, ea_s, adig, ctid, CNT);
-        oz::split_b(Mb, getB, eb_s, bdig, ctid, CNT);
-        cluster.sync();  // every digit is written before any CTA reads them
-        const int ngroup = (T + 7) / 8;
-        for (int task = rank; task < T * ngroup; task += C) {
-          const int ti = task / ngroup, tj = (task % ngroup) * 8 + warp;
-          tile_product(TileJob{Mb, ti, tj, tj < T ? 1 : 0, adig, bdig, ea_s, eb_s, astage,
-                               a.b_prefetch ? bring : nullptr, out});
-        }
-        cluster.sync();
-      };
+      const ZgemmCtx zc{ea_s, eb_s, expart, adig, bdig, stage};
       auto wsym = [&](const double2* Wb, int Mb, int i, int j) {  // symmetric matrix from its upper triangle
         return __ldcg(Wb + (i <= j ? (int64_t)i * Mb + j : (int64_t)j * Mb + i));
       };
 
-      if (!split) {
-        gj(W, M);
-      } else {
-        // X^-1 by its 2 x 2 block form, X = [[A, B], [B^T, D]] with h x h
-        // blocks: two half-size Gauss-Jordan inverses in FP64 (M^3 flops
-        // instead of 4 M^3) and four half-size products on the tensor cores:
-        //   T = A^-1 B,  S = D - B^T T,  Y12 = -T S^-1,  Y11 = A^-1 - Y12 T^T,
-        //   Y22 = S^-1.
-        // A small pivot in either half flags the realization as the full
-        // elimination does.
-        const int h = M >> 1;
-        const int64_t hh = (int64_t)h * h;
-        for (int64_t e = ctid; e < hh; e += CNT) {  // A into Wa (upper triangle)
-          const int i = (int)(e / h), j = (int)(e % h);
-          if (i <= j) Wa[e] = __ldcg(W + (int64_t)i * M + j);
+      // X^-1 by its 2 x 2 block form, X = [[A, B], [B^T, D]] with h x h
+      // blocks, two half-size inverses and four half-size products on the
+      // tensor cores:
+      //   T = A^-1 B,  S = D - B^T T,  Y12 = -T S^-1,  Y11 = A^-1 - Y12 T^T,
+      //   Y22 = S^-1,
+      // with, at two levels, the half-size inverses of A and S in the same
+      // form.  The steps (kInvSteps) act on frames: frame 0 splits X (at W,
+      // row stride M) with the buffers Wa, Tb, Ws; frames 1 and 2 split A^-1's
+      // block Wa and S's block Ws (row stride h) with Wa2, Tb2, Ws2.  Every
+      // Gauss-Jordan block goes through the one call below.  A small pivot in
+      // a block flags the realization as the full elimination does.
+      {
+        const int nsteps = kInvStepCount[split_levels];
+        for (int st = 0; st < nsteps; ++st) {
+          const int code = kInvSteps[split_levels][st];
+          const int op = code >> 2, f = code & 3;
+          double2* P = f == 0 ? W : (f == 1 ? Wa : Ws);
+          const int nP = f == 0 ? M : M >> 1;  // also P's row stride
+          double2* Ha = f == 0 ? Wa : Wa2;
+          double2* Hb = f == 0 ? Tb : Tb2;
+          double2* Hs = f == 0 ? Ws : Ws2;
+          const int h = nP >> 1;
+          const int64_t hh = (int64_t)h * h;
+          if (op == kInvGJ || op == kInvGJA || op == kInvGJS) {
+            gj(op == kInvGJ ? W : (op == kInvGJA ? Ha : Hs), op == kInvGJ ? M : h);
+          } else if (op == kInvCopyA) {  // A into Ha (upper triangle)
+            for (int64_t e = ctid; e < hh; e += CNT) {
+              const int i = (int)(e / h), j = (int)(e % h);
+              if (i <= j) Ha[e] = __ldcg(P + (int64_t)i * nP + j);
+            }
+            cluster.sync();
+          } else if (op == kInvT) {
+            cluster_zgemm(zc, h, Opnd{Ha, h, 0, 1, 0}, Opnd{P, nP, h, 0, 0}, TileOut{Hb, h, 0, 1.0, nullptr, 0, 0, 0, 0});
+          } else if (op == kInvS) {
+            cluster_zgemm(zc, h, Opnd{P, nP, h, 0, 1}, Opnd{Hb, h, 0, 0, 0},
+                          TileOut{Hs, h, 0, -1.0, P, nP, (int64_t)h * nP + h, 0, 1});
+          } else if (op == kInvY12) {
+            cluster_zgemm(zc, h, Opnd{Hb, h, 0, 0, 0}, Opnd{Hs, h, 0, 1, 0}, TileOut{P, nP, h, -1.0, nullptr, 0, 0, 0, 0});
+          } else if (op == kInvY11) {
+            cluster_zgemm(zc, h, Opnd{P, nP, h, 0, 0}, Opnd{Hb, h, 0, 0, 1}, TileOut{P, nP, 0, -1.0, Ha, h, 0, 1, 1});
+          } else {  // kInvY22: Y22 = S^-1
+            for (int64_t e = ctid; e < hh; e += CNT) {
+              const int i = (int)(e / h), j = (int)(e % h);
+              if (i <= j) P[(int64_t)(h + i) * nP + h + j] = __ldcg(Hs + e);
+            }
+            cluster.sync();
+          }
         }
-        cluster.sync();
-        gj(Wa, h);  // Wa = A^-1
-        cluster_zgemm(h, Opnd{Wa, h, 0, 1, 0}, Opnd{W, M, h, 0, 0}, TileOut{Tb, h, 0, 1.0, nullptr, 0, 0, 0, 0});
-        cluster_zgemm(h, Opnd{W, M, h, 0, 1}, Opnd{Tb, h, 0, 0, 0},
-                      TileOut{Ws, h, 0, -1.0, W, M, (int64_t)h * M + h, 0, 1});
-        gj(Ws, h);  // Ws = S^-1
-        cluster_zgemm(h, Opnd{Tb, h, 0, 0, 0}, Opnd{Ws, h, 0, 1, 0}, TileOut{W, M, h, -1.0, nullptr, 0, 0, 0, 0});
-        cluster_zgemm(h, Opnd{W, M, h, 0, 0}, Opnd{Tb, h, 0, 0, 1}, TileOut{W, M, 0, -1.0, Wa, h, 0, 1, 1});
-        for (int64_t e = ctid; e < hh; e += CNT) {  // Y22 = S^-1
-          const int i = (int)(e / h), j = (int)(e % h);
-          if (i <= j) W[(int64_t)(h + i) * M + h + j] = __ldcg(Ws + e);
-        }
-        cluster.sync();
       }
 
       if (gemm_on) {
@@ -764,7 +826,7 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           cluster.sync();  // the new right-hand side is complete before the next slice
         } else {
           // the result overwrites B Gs1 in place (its digits are already taken)
-          cluster_zgemm(M, Opnd{W, M, 0, 1, 0}, Opnd{Rg, M, 0, 0, 0}, TileOut{Rg, M, 0, 1.0, nullptr, 0, 0, 0, 0});
+          cluster_zgemm(zc, M, Opnd{W, M, 0, 1, 0}, Opnd{Rg, M, 0, 0, 0}, TileOut{Rg, M, 0, 1.0, nullptr, 0, 0, 0, 0});
         }
       }
       if (a.state_dump && *status0 != kStatusNeedPivot) {

@@ -473,17 +473,14 @@ bool tensor_r_enabled() {
   return !(e && std::strcmp(e, "0") == 0);
 }
 
-// With the tensor-core product, the 2 x 2 block inverse of the slice matrix
-// (even mode counts from 128 up) unless RG_SPLIT_INVERSE=0.
-bool split_inverse_enabled() {
+// With the tensor-core product, the levels of the 2 x 2 block inverse of the
+// slice matrix (each halves an even mode count of at least 128): 2 unless
+// RG_SPLIT_INVERSE is 0 or 1.
+int split_inverse_levels() {
   const char* e = std::getenv("RG_SPLIT_INVERSE");
-  return !(e && std::strcmp(e, "0") == 0);
-}
-
-// The tensor-core product's B-digit prefetch unless RG_B_PREFETCH=0.
-bool b_prefetch_enabled() {
-  const char* e = std::getenv("RG_B_PREFETCH");
-  return !(e && std::strcmp(e, "0") == 0);
+  if (e && std::strcmp(e, "0") == 0) return 0;
+  if (e && std::strcmp(e, "1") == 0) return 1;
+  return 2;
 }
 
 // Launch arguments for items of this one waveguide (the caller sets nreal,
@@ -498,8 +495,7 @@ rg::SweepArgs make_args(const rg_waveguide* w, int mode) {
   a.symmetric = (w->p.boundtype == RG_BOUND_DIRICHLET && symmetric_enabled()) ? 1 : 0;
   a.sym_tau = symmetric_tau();
   a.tensor_r = tensor_r_enabled() ? 1 : 0;
-  a.split_inverse = split_inverse_enabled() ? 1 : 0;
-  a.b_prefetch = b_prefetch_enabled() ? 1 : 0;
+  a.split_inverse = split_inverse_levels();
   return a;
 }
 
@@ -712,7 +708,7 @@ int run_seed_batch(rg_waveguide* w, const int32_t* d_seeds, int n, double* d_tei
   const int64_t key[kGraphKey] = {n, (int64_t)(intptr_t)d_seeds, (int64_t)(intptr_t)d_teig,
                                   (int64_t)(intptr_t)d_status, (int64_t)(intptr_t)a.work, grid, a.cluster,
                                   a.force_large, a.work_stride, a.symmetric, (int64_t)(intptr_t)a.flag_list,
-                                  tau_bits, a.force_rowsplit, a.force_per_sm, a.tensor_r * 4 + a.split_inverse * 2 + a.b_prefetch};
+                                  tau_bits, a.force_rowsplit, a.force_per_sm, a.tensor_r * 4 + a.split_inverse};
   if (!w->graph || std::memcmp(key, w->graph_key, sizeof key) != 0) {
     if (w->graph) cudaGraphExecDestroy(w->graph);
     w->graph = nullptr;
@@ -884,7 +880,6 @@ int green_view(const rg_waveguide* w, GreenView* out) {
   out->sym_tau = a.sym_tau;
   out->tensor_r = a.tensor_r;
   out->split_inverse = a.split_inverse;
-  out->b_prefetch = a.b_prefetch;
   return RG_OK;
 }
 
@@ -1288,8 +1283,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     a.symmetric = (any_dirichlet && symmetric_enabled()) ? 1 : 0;
     a.sym_tau = symmetric_tau();
     a.tensor_r = tensor_r_enabled() ? 1 : 0;
-    a.split_inverse = split_inverse_enabled() ? 1 : 0;
-    a.b_prefetch = b_prefetch_enabled() ? 1 : 0;
+    a.split_inverse = split_inverse_levels();
     if (maxM > rg::kMaxModesSmem) {
       // The blocked class's makespan is at least its longest item's time on
       // one CTA slot.  When that item's work times the slot count exceeds the
@@ -1338,7 +1332,7 @@ int rg_tdistrib_multi(rg_waveguide* const* wgs, const int32_t* seeds, int n, con
     int64_t tau_bits = 0;
     std::memcpy(&tau_bits, &c.a.sym_tau, sizeof tau_bits);
     const int64_t k[] = {(int64_t)(c.a.item_wg - d_wg), c.a.nreal, c.a.max_M, c.a.max_ny, c.a.symmetric,
-                         c.a.tensor_r * 4 + c.a.split_inverse * 2 + c.a.b_prefetch, c.a.force_cluster, c.a.cluster, c.grid, (int64_t)c.ws_off, c.a.work_stride,
+                         c.a.tensor_r * 4 + c.a.split_inverse, c.a.force_cluster, c.a.cluster, c.grid, (int64_t)c.ws_off, c.a.work_stride,
                          tau_bits};
     key.insert(key.end(), std::begin(k), std::end(k));
   }
