@@ -166,35 +166,26 @@ struct TileOut {
   int aux_sym, upper;
 };
 
-struct BlockJob {
-  int Mb, ti0, tj0;
-  const uint4* adig;
-  const uint4* bdig;
-  const int* ea;
-  const int* eb;
-  uint4* stage;
-  TileOut o;
-};
-
 // One CTA's 2 x 4 block of 16 x 16 output tiles of a cluster product (warp
 // w: row tile ti0 + w/4, column tile tj0 + w%4; both operands' digits staged
-// in shared memory per chunk).  Not inlined: one copy of the tensor-core
-// loop, with its own register allocation, serves all of a slice's products.
-__device__ __noinline__ void block_product(const BlockJob jb) {
-  const TileOut& o = jb.o;
-  oz::gemm_block(jb.Mb, jb.ti0, jb.tj0, o.upper != 0, jb.adig, jb.bdig, jb.ea, jb.eb, jb.stage,
-                 [&](int i, int j, double re, double im) {
-                   if (o.upper && i > j) return;
-                   double2 v = make_double2(o.sign * re, o.sign * im);
-                   if (o.aux) {
-                     const double2 x = o.aux_sym ? __ldcg(o.aux + (i <= j ? (int64_t)i * o.aux_ld + j
-                                                                            : (int64_t)j * o.aux_ld + i))
-                                                 : __ldcg(o.aux + (int64_t)i * o.aux_ld + j + o.aux_off);
-                     v.x += x.x;
-                     v.y += x.y;
-                   }
-                   o.dst[(int64_t)i * o.ld + j + o.off] = v;
-                 });
+// in shared memory per chunk).  The output description o lives in shared
+// memory, so none of its fields holds a register through the tensor-core
+// loop.  Not inlined: one copy of the loop, with its own register
+// allocation, serves all of a slice's products.
+__device__ __noinline__ void block_product(int Mb, int ti0, int tj0, const uint4* adig, const uint4* bdig,
+                                           const int* ea, const int* eb, uint4* stage, const TileOut* o) {
+  oz::gemm_block(Mb, ti0, tj0, o->upper != 0, adig, bdig, ea, eb, stage, [&](int i, int j, double re, double im) {
+    if (o->upper && i > j) return;
+    const double sg = o->sign;
+    double2 v = make_double2(sg * re, sg * im);
+    if (o->aux) {
+      const double2 x = o->aux_sym ? __ldcg(o->aux + (i <= j ? (int64_t)i * o->aux_ld + j : (int64_t)j * o->aux_ld + i))
+                                   : __ldcg(o->aux + (int64_t)i * o->aux_ld + j + o->aux_off);
+      v.x += x.x;
+      v.y += x.y;
+    }
+    o->dst[(int64_t)i * o->ld + j + o->off] = v;
+  });
 }
 
 // Where a cluster product keeps its state: the CTA's exponent arrays in
@@ -254,14 +245,16 @@ __device__ __noinline__ void cluster_zgemm(const ZgemmCtx c, const int Mb, const
   __syncthreads();
   oz::split_a(Mb, getA, c.ea_s, c.adig, ctid, CNT);
   oz::split_b(Mb, getB, c.eb_s, c.bdig, ctid, CNT);
-  cluster.sync();  // every digit is written before any CTA reads them
+  __shared__ TileOut s_out;
+  if (tid == 0) s_out = out;
+  cluster.sync();  // every digit is written before any CTA reads them (and s_out is set)
   const int nbr = (T + oz::kBlkRows - 1) / oz::kBlkRows, nbc = (T + oz::kBlkCols - 1) / oz::kBlkCols;
   int k = 0;
   for (int bi = 0; bi < nbr; ++bi)
     for (int bj = 0; bj < nbc; ++bj) {
       const int ti0 = bi * oz::kBlkRows, tj0 = bj * oz::kBlkCols;
       if (out.upper && ti0 > tj0 + oz::kBlkCols - 1) continue;
-      if (k++ % C == rank) block_product(BlockJob{Mb, ti0, tj0, c.adig, c.bdig, c.ea_s, c.eb_s, c.stage, out});
+      if (k++ % C == rank) block_product(Mb, ti0, tj0, c.adig, c.bdig, c.ea_s, c.eb_s, c.stage, &s_out);
     }
   cluster.sync();
 }
