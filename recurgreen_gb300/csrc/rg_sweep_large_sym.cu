@@ -58,6 +58,10 @@ constexpr int kSymMaxCluster = 8;
 constexpr int kSymMaxRowSplit = 8;
 // The 2 x 2 block inverse for even mode counts from this size up.
 constexpr int kSplitMinModes = 128;
+// Gauss-Jordan blocks of at most this many modes are eliminated in shared
+// memory (gj_small): [n][n+1] matrix, two [n] vectors, [n] flags and the
+// n(n+1)/2 triangle index, within the product staging area.
+constexpr int kSmallGJ = 64;
 
 // The pivot column (panel phase) and the chunk's z values (update phase)
 // share one region: they are never live at the same time.
@@ -81,6 +85,10 @@ struct LargeSymSmem {
                      sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
     return ((b > kStage ? b : kStage) + 15) & ~(size_t)15;
   }
+  static_assert(sizeof(double2) * (kSmallGJ * (kSmallGJ + 1) + 2 * kSmallGJ) +
+                        sizeof(int) * (kSmallGJ + kSmallGJ * (kSmallGJ + 1) / 2) <=
+                    kStage,
+                "the shared-memory Gauss-Jordan block fits the product staging area");
   static size_t bytes(int M, bool tensor) {
     return tensor ? exps_offset(M) + sizeof(int) * 2 * 16 * (size_t)oz::tiles(M) : base(M);
   }
@@ -749,6 +757,118 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           cluster.sync();
         }
       };
+      // Symmetric Gauss-Jordan of an n x n block (n <= kSmallGJ, upper
+      // triangle at P, row stride n) in shared memory: every CTA of the
+      // cluster eliminates the whole block on its own copy (no cluster
+      // barrier per step; the block's FP64 work is small), rank 0 writes the
+      // inverse back.  Step k pivots on the largest unswept diagonal element
+      // (ties: lowest index); with d = 1/M[p][p], r_j = M[p][j] and
+      // g_i = M[i][p] (the swept/unswept sign rule of the blocked sweep),
+      //   M[i][j] -= g_i d r_j (i, j != p),  M[p][j] = d r_j,
+      //   M[i][p] = -g_i d,  M[p][p] = d.
+      // A pivot below sym_tau times the largest unswept entry of its row
+      // flags the realization.  Ends with a cluster barrier.
+      auto gj_small = [&](double2* P, const int nb) {
+        const int ld = nb + 1, ntri = nb * (nb + 1) / 2;
+        double2* Sw = reinterpret_cast<double2*>(stage);  // [nb][ld], upper triangle
+        double2* gcol = Sw + nb * ld;                      // [nb] g_i
+        double2* roww = gcol + nb;                         // [nb] d r_j
+        int* sused = reinterpret_cast<int*>(roww + nb);    // [nb] swept flags
+        int* tri = sused + nb;                             // [ntri] (i << 16) | j
+        __syncthreads();  // the staging area's previous contents have been used
+        for (int e = tid; e < nb * nb; e += NT) {
+          const int i = e / nb, j = e % nb;
+          if (i <= j) Sw[i * ld + j] = __ldcg(P + (int64_t)i * nb + j);
+        }
+        for (int i = tid; i < nb; i += NT) {
+          sused[i] = 0;
+          const int base = i * nb - i * (i - 1) / 2;  // triangle elements of rows < i
+          for (int j = i; j < nb; ++j) tri[base + j - i] = (i << 16) | j;
+        }
+        cluster.sync();  // every CTA has read P before rank 0 overwrites it
+        for (int k = 0; k < nb; ++k) {
+          if (warp == k % NW) {
+            unsigned long long best = 0ULL;
+            int bi = 0x7fffffff;
+            for (int i = lane; i < nb; i += 32) {
+              const unsigned long long key = sused[i] ? 0ULL : pivot_key(Sw[i * ld + i]);
+              if (key > best) {
+                best = key;
+                bi = i;
+              }
+            }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+              const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+              if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+              }
+            }
+            const bool singular = (best == 0ULL);
+            if (singular) {  // zero or NaN diagonal everywhere left: the pivoted kernel decides
+              bi = 0;
+              while (bi < nb - 1 && sused[bi]) ++bi;
+            }
+            const int pk = bi;
+            double2 d = make_double2(0.0, 0.0);
+            if (!singular) {
+              const double2 z = Sw[pk * ld + pk];
+              const double rden = 1.0 / fma(z.x, z.x, z.y * z.y);
+              d = make_double2(z.x * rden, -z.y * rden);
+            }
+            unsigned long long offmax = 0ULL;
+            for (int j = lane; j < nb; j += 32) {
+              double2 rj, gjv;
+              if (j < pk) {
+                const double2 u = Sw[j * ld + pk];
+                rj = sused[j] ? cneg(u) : u;
+                gjv = u;
+              } else {
+                const double2 u = Sw[pk * ld + j];
+                rj = u;
+                gjv = sused[j] ? cneg(u) : u;
+              }
+              if (j != pk && !sused[j]) {
+                const unsigned long long kk2 = pivot_key(rj);
+                offmax = kk2 > offmax ? kk2 : offmax;
+              }
+              gcol[j] = gjv;
+              roww[j] = (j == pk) ? d : cmul(d, rj);
+            }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+              const unsigned long long o2 = __shfl_xor_sync(0xffffffffu, offmax, off);
+              offmax = o2 > offmax ? o2 : offmax;
+            }
+            __syncwarp();  // every lane has read sused[] before lane 0 marks pk
+            if (lane == 0) {
+              const double zmag = __longlong_as_double((long long)best);
+              const double omag = __longlong_as_double((long long)offmax);
+              if (singular || zmag < a.sym_tau * omag) s_status = kStatusNeedPivot;
+              sused[pk] = 1;
+              s_p = pk;
+            }
+          }
+          __syncthreads();
+          const int pk = s_p;
+          for (int e = tid; e < ntri; e += NT) {
+            const int i = tri[e] >> 16, j = tri[e] & 0xffff;
+            const double2 rj = roww[j];
+            const double2 w = (i == pk) ? rj : (j == pk) ? make_double2(0.0, 0.0) : Sw[i * ld + j];
+            const double2 f = (i == pk) ? make_double2(0.0, 0.0) : gcol[i];
+            Sw[i * ld + j] = cfms(w, f, rj);
+          }
+          __syncthreads();
+        }
+        if (rank == 0)
+          for (int e = tid; e < ntri; e += NT) {
+            const int i = tri[e] >> 16, j = tri[e] & 0xffff;
+            P[(int64_t)i * nb + j] = Sw[i * ld + j];
+          }
+        cluster.sync();
+      };
       const ZgemmCtx zc{ea_s, eb_s, expart, adig, bdig, stage};
       auto wsym = [&](const double2* Wb, int Mb, int i, int j) {  // symmetric matrix from its upper triangle
         return __ldcg(Wb + (i <= j ? (int64_t)i * Mb + j : (int64_t)j * Mb + i));
@@ -778,7 +898,10 @@ __global__ void __launch_bounds__(kSymNT, 2) sweep_large_sym_kernel(SweepArgs a)
           const int h = nP >> 1;
           const int64_t hh = (int64_t)h * h;
           if (op == kInvGJ || op == kInvGJA || op == kInvGJS) {
-            gj(op == kInvGJ ? W : (op == kInvGJA ? Ha : Hs), op == kInvGJ ? M : h);
+            double2* Q = op == kInvGJ ? W : (op == kInvGJA ? Ha : Hs);
+            const int nq = op == kInvGJ ? M : h;
+            if (nq <= kSmallGJ) gj_small(Q, nq);
+            else gj(Q, nq);
           } else if (op == kInvCopyA) {  // A into Ha (upper triangle)
             for (int64_t e = ctid; e < hh; e += CNT) {
               const int i = (int)(e / h), j = (int)(e % h);
