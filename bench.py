@@ -63,9 +63,11 @@ BASE = dict(boundtype="dirichlet", nxdiso=2000, nxfree=0, wol=128.25, exfac=1.0,
             dabso=0.0, napera=1.0, naperb=1.0, ny=1024)
 
 # The timed workloads: waveguide parameters, realizations per step, and the
-# slices of the reference arm's per-step sample.
+# slices of the reference arm's per-step sample.  N=256: 304 realizations per
+# step, one per CTA at two CTAs per SM of the GB300's 152 (one wave), where
+# the autotuner's fastest cluster size is one CTA per realization.
 SPECS = {
-    "n256": dict(kw=dict(BASE), batch=152, ref_nx=200,
+    "n256": dict(kw=dict(BASE), batch=304, ref_nx=200,
                  desc="batched N=256: Dirichlet, kW/pi=256.5 (wol=128.25, M=N=256 modes), L/W=1, Nx=2000, "
                       "ny=1024, L/l_s=10, eps=0"),
     "uniform": dict(kw=dict(BASE, wol=32.25, ny=256), batch=4096, ref_nx=2000,
