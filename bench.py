@@ -112,9 +112,9 @@ def executed_flops(M: int, nx: int, kernel: str) -> tuple[float, float]:
         (64 < M <= 512): the inverse in FP64 -- 4 M^3 for one Gauss-Jordan
         sweep; each level of the 2 x 2 block form (even sizes >= 128, at most
         two levels) replaces a size-m inverse by two of size m/2 and four
-        (m/2)^3 products -- and 43 digit pairs x 4 real products x 2 k^3 FP16
-        flops per k x k product: 344 M^3 for the propagator product plus
-        4 x 344 (m/2)^3 per block split;
+        (m/2)^3 products -- and 26 digit pairs x 4 real products x 2 k^3 FP16
+        flops per k x k product: 208 M^3 for the propagator product plus
+        4 x 208 (m/2)^3 per block split;
       * otherwise the pivoted reference count 16 M^3 in FP64.
     RG_TENSOR_R=0 / RG_SPLIT_INVERSE=0 or 1 select the other variants."""
     tensor = os.environ.get("RG_TENSOR_R", "1") != "0" and 64 < M <= 512
@@ -125,11 +125,11 @@ def executed_flops(M: int, nx: int, kernel: str) -> tuple[float, float]:
         return flops_per_realization(M, nx), 0.0
     if not tensor:
         return flops_symmetric(M, nx), 0.0
-    fp16 = 344.0 * M ** 3
+    fp16 = 208.0 * M ** 3
     m, blocks = M, 1
     while want > 0 and m >= 128 and m % 2 == 0:
         want -= 1
-        fp16 += blocks * 4 * 344.0 * (m // 2) ** 3
+        fp16 += blocks * 4 * 208.0 * (m // 2) ** 3
         m, blocks = m // 2, blocks * 2
     fp64 = blocks * 4.0 * m ** 3
     return fp64 * nx, fp16 * nx
@@ -455,7 +455,7 @@ def run_workload(args) -> None:
             rates[name] = v.value
         # the tensor-core complex product (rg_zgemm_batched) at the sweep's
         # sizes: 152 independent M x M products per call, FP16 flops counted as
-        # 43 digit pairs x 4 real products x 2 M^3
+        # 26 digit pairs x 4 real products x 2 M^3
         from recurgreen_gb300.adjoint import _ZGemm
         zrates = {}
         for M in (128, 256, 512):
@@ -473,7 +473,7 @@ def run_workload(args) -> None:
             e1.record()
             e1.synchronize()
             sec = e0.elapsed_time(e1) / 3e3
-            zrates[f"M{M}"] = {"ms_per_call": 1e3 * sec, "fp16_tflops": 43 * 4 * 2 * M ** 3 * nb / sec / 1e12,
+            zrates[f"M{M}"] = {"ms_per_call": 1e3 * sec, "fp16_tflops": 26 * 4 * 2 * M ** 3 * nb / sec / 1e12,
                                "fp64_equivalent_tflops": 8 * M ** 3 * nb / sec / 1e12}
             del A, B, C, zg
         out["clocks"] = clk.stop()

@@ -316,10 +316,10 @@ int rg_probe_rate(int kind, int iters, double* tflops);
 /* No counterpart in the reference: C = A B for M x M complex matrices (host,
  * column-major, 1 <= M <= 512) through the tensor-core path the blocked
  * symmetric sweep uses for its propagator product Gss (B Gs1): each row of A
- * and column of B is cut into eight signed 7-bit digits of a 56-bit fixed
- * point, the digit products run as FP16 mma.sync with exact FP32 level sums,
- * and an exact int64 fold gives C rounded once -- FP64 accuracy (normwise at
- * an FP64 product's level).  For tests and measurements. */
+ * and column of B is cut into six balanced 9-bit digits of a 53-bit fixed
+ * point, 26 digit-pair products run as FP16 mma.sync with exact FP32 level
+ * sums, and an exact int64 fold gives C rounded once -- FP64 accuracy
+ * (normwise at an FP64 product's level).  For tests and measurements. */
 int rg_ozaki_zgemm(int M, const double* a, const double* b, double* c);
 
 /* No counterpart in the reference (the adjoint's per-slice products): for

@@ -66,9 +66,11 @@ constexpr int kSmallGJ = 64;
 // The pivot column (panel phase) and the chunk's z values (update phase)
 // share one region: they are never live at the same time.
 //
-// With tensor_r the product's staged A digits ([2][8][4][32] uint4, 32 KB)
-// and the warps' B prefetch slots (8 x 8 KB) overlay the start of this area
-// (dead during the product), and two arrays of 16-padded exponents follow.
+// With tensor_r the products' two digit stages (72 KB) and, between
+// products, the shared-memory Gauss-Jordan blocks overlay the start of this
+// area (dead during either), and two arrays of 16-padded exponents follow.
+constexpr size_t kSmallGJBytes = sizeof(double2) * (kSmallGJ * (kSmallGJ + 1) + 2 * kSmallGJ) +
+                                 sizeof(int) * (kSmallGJ + kSmallGJ * (kSmallGJ + 1) / 2);
 struct LargeSymSmem {
   __host__ __device__ static size_t shared_region(int M) {
     const size_t z = (size_t)(kSymNT / 4) * 2 * kSymNB;
@@ -78,17 +80,14 @@ struct LargeSymSmem {
     return sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
            sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
   }
-  // both operands' staged digits of a CTA's block of output tiles
-  static constexpr size_t kStage = sizeof(uint4) * oz::kBlkStageUint4;
+  // the products' staged digits, or a shared-memory Gauss-Jordan block
+  static constexpr size_t kStage =
+      sizeof(uint4) * oz::kBlkStageUint4 > kSmallGJBytes ? sizeof(uint4) * oz::kBlkStageUint4 : kSmallGJBytes;
   __host__ __device__ static size_t exps_offset(int M) {
     const size_t b = sizeof(double2) * ((size_t)M * kSymNB + kSymNB * kSymNB + (size_t)M + kSymNB + shared_region(M)) +
                      sizeof(double) * (2 * (size_t)M + 2) + sizeof(int) * 3 * (size_t)M;
     return ((b > kStage ? b : kStage) + 15) & ~(size_t)15;
   }
-  static_assert(sizeof(double2) * (kSmallGJ * (kSmallGJ + 1) + 2 * kSmallGJ) +
-                        sizeof(int) * (kSmallGJ + kSmallGJ * (kSmallGJ + 1) / 2) <=
-                    kStage,
-                "the shared-memory Gauss-Jordan block fits the product staging area");
   static size_t bytes(int M, bool tensor) {
     return tensor ? exps_offset(M) + sizeof(int) * 2 * 16 * (size_t)oz::tiles(M) : base(M);
   }

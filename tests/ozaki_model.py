@@ -1,15 +1,15 @@
 """Exact integer model of the tensor-core complex product (rg_ozaki.cuh).
 
 Test infrastructure: it restates, with numpy integer arithmetic, every step
-of the device path -- row/column exponents, 56-bit rounded fixed point,
-eight signed 7-bit digits, level sums over chunks of 64 complex k, the
-hi/lo int64 fold and the final single rounding -- so the GPU result must
-equal it bit for bit.  Level sums are checked to stay below 2^24 (the
-exactness condition of FP32 accumulation on the tensor cores).
+of the device path -- row/column exponents, 53-bit rounded fixed point, six
+balanced base-512 digits, level sums over chunks of 16 complex k, the hi/lo
+int64 fold and the final single rounding -- so the GPU result must equal it
+bit for bit.  Level sums are checked to stay below 2^24 (the exactness
+condition of FP32 accumulation on the tensor cores).
 """
 import numpy as np
 
-SLICES, LMAX, CHUNK = 8, 8, 64
+SLICES, BITS, LMAX, HI_LEVELS, CHUNK = 6, 9, 6, 3, 16
 NOEXP = -4096
 
 
@@ -20,27 +20,37 @@ def fexp(x: np.ndarray) -> np.ndarray:
     return np.where(eb == 0, NOEXP, eb - 1022)
 
 
-def fixed56(x: np.ndarray, e: np.ndarray) -> np.ndarray:
-    """|x| 2^(56-e) rounded to nearest (ties up), as int64 (< 2^56)."""
+def fixed53(x: np.ndarray, e: np.ndarray) -> np.ndarray:
+    """|x| 2^(53-e) rounded to nearest (ties up), as int64 (< 2^53)."""
     bits = np.ascontiguousarray(x, np.float64).view(np.uint64)
     eb = ((bits >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
     m = ((bits & np.uint64((1 << 52) - 1)) | np.uint64(1 << 52)).astype(np.int64)
-    sh = eb - 1019 - e
+    rs = e - (eb - 1022)
     out = np.zeros(x.shape, np.int64)
-    pos = (eb != 0) & (sh >= 0)
-    out[pos] = m[pos] << sh[pos]
-    neg = (eb != 0) & (sh < 0) & (-sh <= 54)
-    rs = -sh[neg]
-    out[neg] = (m[neg] + (np.int64(1) << (rs - 1))) >> rs
-    assert out.max(initial=0) < (1 << 56)
+    exact = (eb != 0) & (rs == 0)
+    out[exact] = m[exact]
+    shr = (eb != 0) & (rs > 0) & (rs <= 54)
+    r = rs[shr]
+    out[shr] = (m[shr] + (np.int64(1) << (r - 1))) >> r
+    assert out.max(initial=0) < (1 << 53)
     return out
 
 
 def digits(x: np.ndarray, e: np.ndarray):
-    """Signed digits d_p (int64, |d_p| <= 127) of x relative to 2^e (broadcast)."""
-    X = fixed56(x, np.broadcast_to(e, x.shape))
+    """Balanced signed digits d_p (int64, |d_p| <= 256) of x relative to 2^e
+    (broadcast): X = sum_p d_p 2^(9(5-p)), built from the least significant
+    digit up, a digit of 256 or more becoming digit - 512 with a carry."""
+    X = fixed53(x, np.broadcast_to(e, x.shape))
     s = np.where(x < 0, -1, 1)
-    return [((X >> (49 - 7 * p)) & 127) * s for p in range(SLICES)]
+    d = [None] * SLICES
+    carry = np.zeros(X.shape, np.int64)
+    for p in range(SLICES - 1, 0, -1):
+        t = ((X >> (BITS * (SLICES - 1 - p))) & 511) + carry
+        carry = (t >= 256).astype(np.int64)
+        d[p] = t - (carry << 9)
+    d[0] = (X >> (BITS * (SLICES - 1))) + carry
+    assert max(int(np.abs(v).max(initial=0)) for v in d) <= 256
+    return [v * s for v in d]
 
 
 def zgemm(A: np.ndarray, B: np.ndarray) -> np.ndarray:
@@ -71,13 +81,13 @@ def zgemm(A: np.ndarray, B: np.ndarray) -> np.ndarray:
                 vi += Ar[p][:, ks] @ Bi[q][ks, :] + Ai[p][:, ks] @ Br[q][ks, :]
             assert np.abs(vr).max() < (1 << 24) and np.abs(vi).max() < (1 << 24)
             vr, vi = vr.astype(np.int64), vi.astype(np.int64)
-            if lev <= 3:
-                hr += vr << (7 * (3 - lev))
-                hi_ += vi << (7 * (3 - lev))
+            if lev < HI_LEVELS:
+                hr += vr << (BITS * (HI_LEVELS - 1 - lev))
+                hi_ += vi << (BITS * (HI_LEVELS - 1 - lev))
             else:
-                lr += vr << (7 * (8 - lev))
-                li += vi << (7 * (8 - lev))
+                lr += vr << (BITS * (LMAX - lev))
+                li += vi << (BITS * (LMAX - lev))
     e = ea[:, None] + eb[None, :]
-    re = hr.astype(np.float64) * 2.0 ** -35 + lr.astype(np.float64) * 2.0 ** -70
-    im = hi_.astype(np.float64) * 2.0 ** -35 + li.astype(np.float64) * 2.0 ** -70
+    re = hr.astype(np.float64) * 2.0 ** -34 + lr.astype(np.float64) * 2.0 ** -70
+    im = hi_.astype(np.float64) * 2.0 ** -34 + li.astype(np.float64) * 2.0 ** -70
     return np.ldexp(re, e) + 1j * np.ldexp(im, e)
