@@ -85,28 +85,18 @@ __global__ void __launch_bounds__(kOzThreads) zb_split_kernel(int M, ZOp A, ZOp 
   oz::split_b(M, [&](int k, int j) { return zscale(rowscale, k, zat(B, item, M, k, j)); }, w.eb, w.bdig, t0, step);
 }
 
-// CTA (item, row tile ti, group of 8 column tiles); warp w takes column
-// tile 8 group + w.  C = alpha (A B) + beta D.
+// CTA (item, block of 2 x 4 output tiles): oz::gemm_block with both
+// operands' digits staged in shared memory.  C = alpha (A B) + beta D.
 __global__ void __launch_bounds__(kOzThreads, 2) zb_gemm_kernel(int M, char* ws, double2 alpha, ZOp D, double beta,
                                                                 double2* C, int64_t strideC, int colmajor) {
-  __shared__ uint4 astage[2 * oz::kSlices * oz::kChunkTiles * 32];
+  extern __shared__ uint4 stg[];
   const int T = oz::tiles(M);
-  const int ngroup = (T + 7) / 8;
-  const int item = blockIdx.x / (T * ngroup), rest = blockIdx.x % (T * ngroup);
-  const int ti = rest / ngroup, tj = (rest % ngroup) * 8 + (threadIdx.x >> 5);
+  const int nbr = (T + oz::kBlkRows - 1) / oz::kBlkRows, nbc = (T + oz::kBlkCols - 1) / oz::kBlkCols;
+  const int item = blockIdx.x / (nbr * nbc), rest = blockIdx.x % (nbr * nbc);
+  const int ti0 = (rest / nbc) * oz::kBlkRows, tj0 = (rest % nbc) * oz::kBlkCols;
   const ItemWs w = item_ws(ws, M, item);
-  const int64_t plane = (int64_t)T * T * 32;
-  auto stage = [&](int ch) {
-    __syncthreads();
-    const int nk = min(oz::kChunkTiles, T - ch * oz::kChunkTiles);
-    for (int e = threadIdx.x; e < 2 * oz::kSlices * oz::kChunkTiles * 32; e += blockDim.x) {
-      const int lane = e & 31, kk = (e >> 5) % oz::kChunkTiles, ps = (e >> 5) / oz::kChunkTiles;
-      if (kk < nk) astage[e] = w.adig[ps * plane + ((int64_t)ti * T + ch * oz::kChunkTiles + kk) * 32 + lane];
-    }
-    __syncthreads();
-  };
   double2* c = C + (int64_t)item * strideC;
-  oz::gemm_tile(M, ti, tj, tj < T, w.bdig, w.ea, w.eb, astage, nullptr, stage, [&](int i, int j, double re, double im) {
+  oz::gemm_block(M, ti0, tj0, false, w.adig, w.bdig, w.ea, w.eb, stg, [&](int i, int j, double re, double im) {
     double2 v = make_double2(alpha.x * re - alpha.y * im, alpha.x * im + alpha.y * re);
     if (beta != 0.0) {
       const double2 d = zat(D, item, M, i, j);
@@ -117,13 +107,17 @@ __global__ void __launch_bounds__(kOzThreads, 2) zb_gemm_kernel(int M, char* ws,
   });
 }
 
+constexpr size_t kZbGemmSmem = sizeof(uint4) * oz::kBlkStageUint4;
+
 int launch_zgemm(int M, int nbatch, const ZOp& A, const ZOp& B, const double2* rowscale, double2 alpha, const ZOp& D,
                  double beta, double2* C, int64_t strideC, int colmajor, char* ws, cudaStream_t s) {
   const int T = oz::tiles(M);
   const int per = std::max(1, std::min(16, T * T * 32 / kOzThreads));
   zb_exps_kernel<<<nbatch, kOzThreads, 0, s>>>(M, A, B, rowscale, ws);
   zb_split_kernel<<<nbatch * per, kOzThreads, 0, s>>>(M, A, B, rowscale, ws, per);
-  zb_gemm_kernel<<<nbatch * T * ((T + 7) / 8), kOzThreads, 0, s>>>(M, ws, alpha, D, beta, C, strideC, colmajor);
+  RG_CUDA(cudaFuncSetAttribute(zb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZbGemmSmem));
+  const int nblk = ((T + oz::kBlkRows - 1) / oz::kBlkRows) * ((T + oz::kBlkCols - 1) / oz::kBlkCols);
+  zb_gemm_kernel<<<nbatch * nblk, kOzThreads, kZbGemmSmem, s>>>(M, ws, alpha, D, beta, C, strideC, colmajor);
   RG_CUDA(cudaGetLastError());
   return RG_OK;
 }

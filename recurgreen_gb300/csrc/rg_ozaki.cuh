@@ -57,7 +57,6 @@ constexpr int kDigitBits = 9;   // base 2^9, balanced digits in [-256, 256]
 constexpr int kFixedBits = 53;  // fixed-point bits of an entry
 constexpr int kLmax = 6;        // highest level kept
 constexpr int kHiLevels = 3;    // levels 0..2 fold into hi, 3..6 into lo
-constexpr int kChunkTiles = 1;  // k tiles (of 16 complex k) per fold
 constexpr int kNoExp = -4096;   // exponent of zero rows
 // C = 2^(ea+eb) (hi kHiScale + lo kLoScale)
 constexpr double kHiScale = 0x1p-34;  // 2^-(16 + 9 (kHiLevels - 1))
@@ -219,125 +218,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // all but the most recently committed group complete
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// uint4 of one warp's B prefetch buffer: two slots of [2 parts][kChunkTiles][32 lanes].
-constexpr int kBringUint4 = 2 * 2 * kChunkTiles * 32;
-
-// One warp's 16 x 16 complex tile (ti, tj) of C = A B over all k.  The A
-// digits of the current chunk come from shared memory (astage: [2][8][4][32]
-// uint4, filled by the caller's stage for this row tile and chunk); the B
-// digits come from global memory (L2).  With bring (this warp's kBringUint4
-// uint4 of shared memory), the B digits of the next digit pair are copied
-// into the other of two slots with cp.async while the current pair's
-// products run, so the L2 latency overlaps the tensor-core work; each lane
-// copies and reads only its own 16-byte elements.  `stage` is called with
-// the chunk index before the chunk's products and must leave astage filled
-// for every warp (it synchronises the CTA).  out(i, j, re, im) stores C_ij.
-template <class Stage, class Out>
-__device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig, const int* ea, const int* eb,
-                          const uint4* astage, uint4* bring, Stage stage, Out out) {
-  const int T = tiles(M);
-  const int lane = threadIdx.x & 31;
-  const int64_t bplane = (int64_t)T * T * 32;
-  long long hi[16], lo[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) hi[k] = lo[k] = 0;
-  const int nchunk = (T + kChunkTiles - 1) / kChunkTiles;
-  // the B digits of (chunk ch, slice q) into slot `slot` of bring
-  auto fetch = [&](int ch, int q, int slot) {
-    const int nk = min(kChunkTiles, T - ch * kChunkTiles);
-    const uint4* src = bdig + ((int64_t)tj * T + ch * kChunkTiles) * 32 + lane;
-    uint4* dst = bring + slot * (2 * kChunkTiles * 32) + lane;
-#pragma unroll
-    for (int part = 0; part < 2; ++part)
-#pragma unroll
-      for (int kk = 0; kk < kChunkTiles; ++kk)
-        if (kk < nk) cp_async16(dst + (part * kChunkTiles + kk) * 32, src + (int64_t)(part * kSlices + q) * bplane + kk * 32);
-    cp_async_commit();
-  };
-  int slot = 0;
-  if (active && bring) fetch(0, 0, 0);
-  for (int ch = 0; ch < nchunk; ++ch) {
-    stage(ch);
-    const int nk = min(kChunkTiles, T - ch * kChunkTiles);
-    if (active) {
-      const uint4* bbase = bdig + ((int64_t)tj * T + ch * kChunkTiles) * 32 + lane;
-#pragma unroll 1
-      for (int l = 0; l <= kLmax; ++l) {
-        float acc[4][4];  // [re n0, re n1, im n0, im n1][4]
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int w = 0; w < 4; ++w) acc[u][w] = 0.0f;
-        const int p0 = max(0, l - (kSlices - 1)), p1 = min(l, kSlices - 1);
-#pragma unroll 1
-        for (int p = p0; p <= p1; ++p) {
-          const int q = l - p;
-          const uint4* cur = nullptr;
-          if (bring) {
-            // this pair's B digits have landed in `slot`; start copying the
-            // next pair's (possibly of the next chunk) into the other slot
-            cp_async_wait_all();
-            cur = bring + slot * (2 * kChunkTiles * 32) + lane;
-            int nl = l, np = p + 1, nch = ch;
-            if (np > p1) {
-              nl = l + 1;
-              if (nl > kLmax) {
-                nl = 0;
-                ++nch;
-              }
-              np = max(0, nl - (kSlices - 1));
-            }
-            if (nch < nchunk) fetch(nch, nl - np, slot ^ 1);
-          }
-          const uint4* ar = astage + (p * kChunkTiles) * 32 + lane;
-          const uint4* ai = astage + ((kSlices + p) * kChunkTiles) * 32 + lane;
-#pragma unroll
-          for (int kk = 0; kk < kChunkTiles; ++kk) {
-            if (kk < nk) {
-              const uint4 vb = cur ? cur[kk * 32] : __ldcg(bbase + (int64_t)q * bplane + kk * 32);
-              const uint4 vc = cur ? cur[(kChunkTiles + kk) * 32] : __ldcg(bbase + (int64_t)(kSlices + q) * bplane + kk * 32);
-              const uint4 var = ar[kk * 32], vai = ai[kk * 32];
-              // re += Ar Br - Ai Bi; im += Ar Bi + Ai Br
-              mma16816(acc[0], var, vb.x, vb.y);
-              mma16816(acc[0], vai, vc.x ^ 0x80008000u, vc.y ^ 0x80008000u);
-              mma16816(acc[1], var, vb.z, vb.w);
-              mma16816(acc[1], vai, vc.z ^ 0x80008000u, vc.w ^ 0x80008000u);
-              mma16816(acc[2], var, vc.x, vc.y);
-              mma16816(acc[2], vai, vb.x, vb.y);
-              mma16816(acc[3], var, vc.z, vc.w);
-              mma16816(acc[3], vai, vb.z, vb.w);
-            }
-          }
-          slot ^= 1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int w = 0; w < 4; ++w) {
-            const long long v = (long long)__float2int_rn(acc[u][w]);
-            if (l < kHiLevels) hi[u * 4 + w] += v << (kDigitBits * (kHiLevels - 1 - l));
-            else lo[u * 4 + w] += v << (kDigitBits * (kLmax - l));
-          }
-      }
-    }
-  }
-  if (!active) return;
-  const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-  for (int n = 0; n < 2; ++n)
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      const int i = ti * 16 + g + ((w & 2) ? 8 : 0);
-      const int j = tj * 16 + n * 8 + 2 * t + (w & 1);
-      if (i < M && j < M) {
-        const int e = ea[i] + eb[j];
-        const double re = fma((double)hi[n * 4 + w], kHiScale, (double)lo[n * 4 + w] * kLoScale);
-        const double im = fma((double)hi[8 + n * 4 + w], kHiScale, (double)lo[8 + n * 4 + w] * kLoScale);
-        out(i, j, scalbn(re, e), scalbn(im, e));
-      }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // The CTA-blocked product: a CTA of 8 warps computes a 2 x 4 block of 16 x 16
 // complex tiles (warp w: row tile ti0 + w/4, column tile tj0 + w%4).  Both
@@ -346,10 +226,10 @@ __device__ void gemm_tile(int M, int ti, int tj, bool active, const uint4* bdig,
 // stages deep (stg: kBlkStageUint4 uint4 = 72 KB), so the copy of k tile
 // t + 1 runs while the tensor cores work on k tile t and the loop reads no
 // global memory; every staged A digit serves 4 tiles and every B digit 2.
-// The level sums of a k tile are folded after it (kChunkTiles = 1).  With
+// The level sums of a k tile are folded after it.  With
 // `upper`, warps whose tile lies wholly below the diagonal (ti > tj) skip the
-// products (their outputs are not wanted).  out(i, j, re, im) as in
-// gemm_tile.
+// products (their outputs are not wanted).  out(i, j, re, im) stores C_ij
+// (called for i, j < M only).
 // ---------------------------------------------------------------------------
 constexpr int kBlkRows = 2, kBlkCols = 4;
 constexpr int kBlkAUint4 = kBlkRows * 2 * kSlices * 32;                 // one stage's A digits
