@@ -96,14 +96,15 @@ struct LargeSymSmem {
 // Workspace of one cluster, in double2 units: W, R, t (M x M each), the
 // generator states (ny x 4 uint64), the paired potential row (ny doubles)
 // and each CTA's raw pivot columns (kSymMaxCluster x NB x M).
-// With tensor_r the digit planes of both product operands and each CTA's
-// partial exponents ([kSymMaxCluster][2][16 T] ints) follow.
+// With tensor_r the digit planes of both product operands and the cluster's
+// exponent exchange area ([kSymMaxCluster][2][16 T] ints) follow.
 __host__ __device__ inline int64_t large_sym_base_stride(int M, int ny) {
   const int64_t mm = (int64_t)M * M;
   const int64_t urow = ((int64_t)ny + 1) / 2;
   return ((3 * mm + 2 * (int64_t)ny + urow + (int64_t)kSymMaxCluster * kSymNB * M) + 15) & ~(int64_t)15;
 }
-// Then the 2 x 2 block inverse's three h x h buffers (h = M / 2).
+// Then the 2 x 2 block inverse's buffers: three h x h (h = M / 2) for the
+// first level, three (h/2) x (h/2) for the second.
 __host__ __device__ inline int64_t large_sym_schur_offset(int M, int ny) {
   const int64_t ex = ((int64_t)kSymMaxCluster * 2 * 16 * oz::tiles(M) * 4 + 15) / 16;
   return (large_sym_base_stride(M, ny) + 2 * oz::operand_uint4(M) + ex + 15) & ~(int64_t)15;
@@ -126,8 +127,8 @@ __host__ __device__ inline int split_depth(int want, int M) {
 }
 
 // The steps of the symmetric inverse for 0, 1 and 2 block levels: code =
-// op * 4 + frame (frame 0: X itself; 1: the block A^-1 of frame 0; 2: its
-// block S).
+// op * 4 + frame (frame 0: X itself; 1: frame 0's block A, inverted in place
+// in its buffer; 2: frame 0's Schur complement S, likewise).
 enum : int { kInvGJ, kInvCopyA, kInvGJA, kInvT, kInvS, kInvGJS, kInvY12, kInvY11, kInvY22 };
 #define RG_INV(op, f) (unsigned char)((op) * 4 + (f))
 __constant__ unsigned char kInvSteps[3][22] = {
