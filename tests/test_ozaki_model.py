@@ -45,3 +45,24 @@ def test_model_zero_rows_and_extremes():
     assert np.all(oz[3, :] == 0) and np.all(oz[:, 5] == 0)
     ex = A.astype(np.clongdouble) @ B.astype(np.clongdouble)
     assert float(np.linalg.norm(oz - ex) / np.linalg.norm(ex)) < 1e-15
+
+
+def test_balanced_digits_reconstruct_the_fixed_point():
+    """The six balanced base-512 digits rebuild the 53-bit fixed point exactly
+    and stay within [-256, 256], including all-carry patterns (raw digits of
+    256 and 511 everywhere) and the largest and smallest entries of a row."""
+    e = np.int64(0)
+    # X = |x| 2^(53-e) for x in [0.5, 1) (exponent 0): X spans [2^52, 2^53)
+    raw = [(1 << 53) - 1,                      # every raw digit 511 except the top
+           sum(256 << (9 * k) for k in range(5)) | (1 << 52),  # every low raw digit exactly 256
+           sum(255 << (9 * k) for k in range(5)) | (1 << 52),  # every low raw digit 255: no carry
+           1 << 52]
+    xs = np.array([X * 2.0 ** -53 for X in raw] + [-0.75, 1e-12, 2.0 ** -60, 0.0])
+    ds = OZ.digits(xs, np.full(xs.shape, e))
+    X = OZ.fixed53(xs, np.full(xs.shape, e))
+    rebuilt = sum(d * (1 << (9 * (OZ.SLICES - 1 - p))) for p, d in enumerate(ds))
+    assert np.array_equal(np.abs(rebuilt), X)
+    assert np.array_equal(rebuilt < 0, (xs < 0) & (X > 0))
+    assert max(int(np.abs(d).max()) for d in ds) <= 256
+    # the exactly representable raw values survive the rounding to 53 bits unchanged
+    assert [int(v) for v in X[:4]] == raw
