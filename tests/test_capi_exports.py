@@ -59,3 +59,24 @@ def test_histogram_rejects_unsorted_bins_on_host(libso):
     libso.rg_histogram.argtypes = [dp, ctypes.c_int64, dp, ctypes.c_int, dp, dp]
     rc = libso.rg_histogram(s.ctypes.data_as(dp), 1, b.ctypes.data_as(dp), 3, h.ctypes.data_as(dp), ctypes.byref(m))
     assert rc == rg.RG_ERR_INVALID_ARG
+
+
+def test_zgemm_workspace_size_follows_the_digit_layout(libso):
+    """rg_zgemm_workspace_bytes (host arithmetic, no GPU): per product, both
+    operands' digit planes -- 2 parts x 6 slices of FP16 digits, i.e. 24 bytes
+    per entry of each operand, in 16 x 16 tiles -- and the row and column
+    exponents (16-byte padded); -1 outside 1 <= M <= 512."""
+    f = libso.rg_zgemm_workspace_bytes
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int, ctypes.c_int]
+
+    def expected(M, nbatch):
+        T = (M + 15) // 16
+        operand = 2 * 6 * T * T * 32 * 16  # uint4 per lane per tile per plane
+        exps = (2 * T * 16 * 4 + 15) // 16 * 16
+        return nbatch * (2 * operand + exps)
+
+    for M, nb in ((1, 1), (64, 5), (100, 2), (128, 3), (512, 1)):
+        assert f(M, nb) == expected(M, nb), M
+    assert expected(128, 1) == 2 * 24 * 128 * 128 + 1024
+    assert f(0, 1) == -1 and f(513, 1) == -1 and f(16, -1) == -1
